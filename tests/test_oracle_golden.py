@@ -1,0 +1,87 @@
+"""The CPU oracle against the golden vectors made by running the reference's
+own kernels and host code (tests/golden/make_golden.py): bit-exact for BFS,
+SSSP, CC and the reference PageRank, on RMAT graphs and hand-built edge cases,
+under every static/on-demand split the fixtures hold."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+
+
+def _oracle_run(z, algo, source):
+    if algo == "bfs":
+        return oracle.bfs(z["ptr"], z["col"], source)
+    if algo == "sssp":
+        return oracle.sssp(z["ptr"], z["adj"], source)
+    if algo == "cc":
+        return oracle.cc(z["sptr"], z["scol"])
+    return oracle.pr_ref(z["cptr"], z["ccol"], z["outdeg"])[0]
+
+
+@pytest.mark.parametrize("graph", sorted(MANIFEST["graphs"]))
+def test_oracle_matches_reference_golden(graph):
+    z = np.load(os.path.join(GOLDEN, graph + ".npz"))
+    cache = {}
+    runs = MANIFEST["graphs"][graph]["runs"]
+    assert runs
+    for r in runs:
+        k = (r["algo"], r["source"])
+        if k not in cache:
+            cache[k] = _oracle_run(z, *k)
+        exp = z[r["key"]]
+        assert exp.dtype == cache[k].dtype
+        assert np.array_equal(exp, cache[k]), r["key"]
+
+
+def test_golden_records_the_static_pointer_hazard():
+    """The reference leaves staticNodePointer[max_static_node] unset
+    (GraphMeta.cuh:230-233). The fixtures keep its as-is output too; it differs
+    from the intended result only in runs that have a static region at all
+    (a fully static graph still leaves its last static vertex unset)."""
+    seen = 0
+    for g, v in MANIFEST["graphs"].items():
+        z = np.load(os.path.join(GOLDEN, g + ".npz"))
+        for r in v["runs"]:
+            differs = not np.array_equal(z[r["key"]], z[r["key"] + "_asis"])
+            assert differs == (r["asis_differs"] > 0)
+            if differs:
+                seen += 1
+                assert r["static_edges"] > 0
+    assert seen > 0
+
+
+def test_static_split_rule():
+    z = np.load(os.path.join(GOLDEN, "zero_degree_ends.npz"))
+    flags, mps, ins = oracle.static_split(z["ptr"], 5000)
+    assert mps == 4096
+    # vertex 0 sits at offset 0 with degree 0: the u64 test wraps, not static
+    assert flags[0] == 0
+    assert ins == int(z["ptr"][-1])
+
+
+def test_pr_std_converges_and_sums_to_one():
+    z = np.load(os.path.join(GOLDEN, "rmat_s10_ef16_seed1.npz"))
+    r, it, res = oracle.pr_std(z["cptr"], z["ccol"], z["outdeg"])
+    assert abs(r.sum() - 1.0) < 1e-9
+    assert res < 1e-9 and it < 100
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_threaded_reference_scheme_matches_oracle(mode):
+    z = np.load(os.path.join(GOLDEN, "rmat_s11_ef8_seed2.npz"))
+    if mode == 0:
+        exp = oracle.bfs(z["ptr"], z["col"], 1)
+        got, _ = oracle.relax_mt(0, z["ptr"], z["col"], 1, 4)
+    elif mode == 1:
+        exp = oracle.sssp(z["ptr"], z["adj"], 1)
+        got, _ = oracle.relax_mt(1, z["ptr"], z["adj"], 1, 4)
+    else:
+        exp = oracle.cc(z["sptr"], z["scol"])
+        got, _ = oracle.relax_mt(2, z["sptr"], z["scol"], 0, 4)
+    assert np.array_equal(exp, got)
