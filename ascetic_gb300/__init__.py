@@ -1,0 +1,315 @@
+"""ascetic_gb300: GB300-native out-of-GPU-memory graph iteration engine.
+
+A thin ctypes mirror of the C ABI in include/ascetic.h (libascetic_gb300.so,
+built in-tree by ascetic_gb300/build.py). The reference's host drivers
+bfs_opt / cc_opt / sssp_opt / pr_opt (CalculateOpt.cuh:11-14) map to
+``bfs_opt`` ... ``pr_opt`` here; ``Graph`` mirrors GraphMeta (GraphMeta.cuh:52-149).
+
+The library loads lazily: importing this package never touches the GPU, and
+every call that needs the engine raises ``EngineUnavailable`` when the shared
+library has not been built. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import formats  # noqa: F401  (re-exported helper module)
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libascetic_gb300.so")
+PTGRAPH_PATH = os.path.join(_PKG, "_lib", "ptgraph")
+
+# enums (include/ascetic.h)
+OK, ERR_INVALID, ERR_BAD_FILE, ERR_BUDGET, ERR_CUDA, ERR_TIMEOUT, ERR_CANCELLED, ERR_UNSUPPORTED, \
+    ERR_NO_DEVICE, ERR_NOMEM, ERR_BUSY = range(11)
+FMT_AUTO, FMT_BCSR, FMT_BWCSR, FMT_BCSC, FMT_BCSR32 = range(5)
+BFS, SSSP, CC, PR = range(4)
+BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES = range(5)
+PR_REF, PR_STD = 0, 1
+F64, F32 = 0, 1
+RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING = 1, 2, 4
+RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
+ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
+
+# every symbol include/ascetic.h declares
+EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_count", "asc_budget_default",
+            "asc_graph_open", "asc_graph_from_csr", "asc_graph_info_get", "asc_graph_close",
+            "asc_params_default", "asc_run", "asc_bfs_opt", "asc_cc_opt", "asc_sssp_opt", "asc_pr_opt",
+            "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe"]
+
+
+class EngineUnavailable(RuntimeError):
+    pass
+
+
+class AscError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_status_name(status), msg))
+        self.status = status
+
+
+class Budget(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_uint32), ("fragment_edges", ctypes.c_uint32), ("value", ctypes.c_double)]
+
+
+class GraphInfo(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_uint64), ("edges", ctypes.c_uint64), ("edge_bytes", ctypes.c_uint32),
+                ("is_csc", ctypes.c_uint32), ("static_edges", ctypes.c_uint64),
+                ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
+                ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
+                ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("pr_mode", ctypes.c_uint32), ("precision", ctypes.c_uint32), ("damping", ctypes.c_double),
+                ("tolerance", ctypes.c_double), ("max_iterations", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("status_detail", ctypes.c_int32),
+                ("frontier_vertices", ctypes.c_uint64), ("ondemand_vertices", ctypes.c_uint64),
+                ("edges_processed", ctypes.c_uint64),
+                ("ondemand_edges", ctypes.c_uint64), ("ondemand_bytes", ctypes.c_uint64),
+                ("reached_vertices", ctypes.c_uint64), ("reached_edges", ctypes.c_uint64),
+                ("ms_total", ctypes.c_double), ("ms_static", ctypes.c_double), ("ms_ondemand", ctypes.c_double),
+                ("ms_copyout", ctypes.c_double), ("residual", ctypes.c_double),
+                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "status_detail")}
+
+
+_lib = None
+
+
+def _status_name(s):
+    names = ["OK", "ERR_INVALID", "ERR_BAD_FILE", "ERR_BUDGET", "ERR_CUDA", "ERR_TIMEOUT", "ERR_CANCELLED",
+             "ERR_UNSUPPORTED", "ERR_NO_DEVICE", "ERR_NOMEM", "ERR_BUSY"]
+    return names[s] if 0 <= s < len(names) else "status %d" % s
+
+
+def lib():
+    """Loads libascetic_gb300.so; raises EngineUnavailable when it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise EngineUnavailable("%s is not built: run ascetic_gb300/build.py (nvcc, sm_103a)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    c_u32, c_u64, c_dbl, c_vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p
+    gpp = P(c_vp)
+    sig = {
+        "asc_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "asc_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
+        "asc_version": ([], ctypes.c_char_p),
+        "asc_device_count": ([], ctypes.c_int),
+        "asc_budget_default": ([P(Budget)], None),
+        "asc_graph_open": ([ctypes.c_char_p, ctypes.c_int, P(Budget), gpp], ctypes.c_int),
+        "asc_graph_from_csr": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, P(Budget), gpp], ctypes.c_int),
+        "asc_graph_info_get": ([c_vp, P(GraphInfo)], ctypes.c_int),
+        "asc_graph_close": ([c_vp], ctypes.c_int),
+        "asc_params_default": ([P(Params)], None),
+        "asc_run": ([c_vp, ctypes.c_int, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
+        "asc_bfs_opt": ([ctypes.c_char_p, c_u32, c_dbl, c_vp, P(Stats)], ctypes.c_int),
+        "asc_cc_opt": ([ctypes.c_char_p, c_dbl, c_vp, P(Stats)], ctypes.c_int),
+        "asc_sssp_opt": ([ctypes.c_char_p, c_u32, c_dbl, c_vp, P(Stats)], ctypes.c_int),
+        "asc_pr_opt": ([ctypes.c_char_p, c_dbl, c_vp, P(Stats)], ctypes.c_int),
+        "asc_rmat_csr": ([c_u32, c_u32, c_u64, c_dbl, c_dbl, c_dbl, c_u32, c_u32, c_u32, c_vp, c_vp, c_vp],
+                         ctypes.c_int),
+        "asc_graph_rmat": ([c_u32, c_u32, c_u64, c_dbl, c_dbl, c_dbl, c_u32, c_u32, c_u32, P(Budget), gpp],
+                           ctypes.c_int),
+        "asc_write_graph": ([ctypes.c_char_p, ctypes.c_int, c_u64, c_u64, c_vp, c_vp, c_vp], ctypes.c_int),
+        "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().asc_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(status):
+    if status != OK:
+        raise AscError(status, last_error())
+
+
+def device_count():
+    return lib().asc_device_count()
+
+
+def make_budget(frac=None, nbytes=None, edges=None, advise_k=None, fragment_edges=4096):
+    b = Budget()
+    lib().asc_budget_default(ctypes.byref(b))
+    b.fragment_edges = fragment_edges
+    if frac is not None:
+        b.mode, b.value = BUDGET_FRAC, float(frac)
+    elif nbytes is not None:
+        b.mode, b.value = BUDGET_BYTES, float(nbytes)
+    elif edges is not None:
+        b.mode, b.value = BUDGET_EDGES, float(edges)
+    elif advise_k is not None:
+        b.mode, b.value = BUDGET_ADVISE_K, float(advise_k)
+    return b
+
+
+def make_params(pr_mode=PR_REF, precision=F64, damping=0.85, tolerance=1e-9, max_iterations=0, flags=0):
+    p = Params()
+    lib().asc_params_default(ctypes.byref(p))
+    p.pr_mode, p.precision, p.damping, p.tolerance = pr_mode, precision, damping, tolerance
+    p.max_iterations, p.flags = max_iterations, flags
+    return p
+
+
+class Graph:
+    """A graph resident as a device static prefix plus a pinned host copy."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+        info = GraphInfo()
+        _check(lib().asc_graph_info_get(self._h, ctypes.byref(info)))
+        self.info = info
+        self.V = info.vertices
+        self.E = info.edges
+
+    @classmethod
+    def open(cls, path, fmt=FMT_AUTO, budget=None):
+        h = ctypes.c_void_p()
+        b = budget if budget is not None else make_budget()
+        _check(lib().asc_graph_open(path.encode(), fmt, ctypes.byref(b), ctypes.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_csr(cls, ptr, edges, outdeg=None, budget=None):
+        """ptr: V+1 offsets; edges: u32 destinations, or (E, 2) u32 (dst, weight)."""
+        ptr = np.ascontiguousarray(ptr, dtype=np.uint64)
+        edges = np.ascontiguousarray(edges, dtype=np.uint32)
+        V = len(ptr) - 1
+        E = int(ptr[-1])
+        eb = 8 if edges.ndim == 2 else 4
+        if edges.size == 0:
+            edges = np.zeros(2, np.uint32)
+        od = None
+        if outdeg is not None:
+            od = np.ascontiguousarray(outdeg, dtype=np.uint32)
+        b = budget if budget is not None else make_budget()
+        h = ctypes.c_void_p()
+        _check(lib().asc_graph_from_csr(V, E, ptr.ctypes.data, edges.ctypes.data, eb,
+                                        od.ctypes.data if od is not None else None, ctypes.byref(b),
+                                        ctypes.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def rmat(cls, scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19, weights=None, symmetric=False,
+             transpose=False, budget=None):
+        flags = (RMAT_WEIGHTS if weights else 0) | (RMAT_SYMMETRIC if symmetric else 0) | \
+            (RMAT_TRANSPOSE if transpose else 0)
+        wmin, wmax = weights if weights else (0, 0)
+        bud = budget if budget is not None else make_budget()
+        h = ctypes.c_void_p()
+        _check(lib().asc_graph_rmat(scale, edge_factor, seed, a, b, c, wmin, wmax, flags, ctypes.byref(bud),
+                                    ctypes.byref(h)))
+        return cls(h.value)
+
+    def close(self):
+        if self._h:
+            lib().asc_graph_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def refresh_info(self):
+        _check(lib().asc_graph_info_get(self._h, ctypes.byref(self.info)))
+        return self.info
+
+    def run(self, algo, source=0, params=None, out=None, no_output=False):
+        """Runs one query; returns (values, stats dict)."""
+        if isinstance(algo, str):
+            algo = ALGOS[algo]
+        p = params if params is not None else make_params()
+        if no_output:
+            p.flags |= RUN_NO_OUTPUT
+        if out is None and not no_output:
+            if algo == PR:
+                out = np.empty(self.V, np.float32 if (p.precision == F32 and p.pr_mode == PR_STD) else np.float64)
+            else:
+                out = np.empty(self.V, np.uint32)
+        st = Stats()
+        _check(lib().asc_run(self._h, algo, source, ctypes.byref(p),
+                             out.ctypes.data if out is not None else None, ctypes.byref(st)))
+        return out, st.as_dict()
+
+
+def rmat_csr(scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19, weights=None, symmetric=False,
+             transpose=False):
+    """Host-only RMAT generator (no GPU needed): returns ptr, edges[, outdeg]."""
+    V = 1 << scale
+    E = V * edge_factor * (2 if symmetric else 1)
+    flags = (RMAT_WEIGHTS if weights else 0) | (RMAT_SYMMETRIC if symmetric else 0) | \
+        (RMAT_TRANSPOSE if transpose else 0)
+    wmin, wmax = weights if weights else (0, 0)
+    ptr = np.empty(V + 1, np.uint64)
+    edges = np.empty((E, 2) if weights else E, np.uint32)
+    outdeg = np.empty(V, np.uint32) if transpose else None
+    _check(lib().asc_rmat_csr(scale, edge_factor, seed, a, b, c, wmin, wmax, flags, ptr.ctypes.data,
+                              edges.ctypes.data, outdeg.ctypes.data if outdeg is not None else None))
+    return (ptr, edges, outdeg) if transpose else (ptr, edges)
+
+
+def link_probe(nbytes=1 << 30, iters=5):
+    """(pinned H2D copy-engine GB/s, SM zero-copy read GB/s)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib().asc_link_probe(nbytes, iters, ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
+
+
+def write_graph(path, fmt, ptr, edges, outdeg=None):
+    ptr = np.ascontiguousarray(ptr, dtype=np.uint64)
+    edges = np.ascontiguousarray(edges, dtype=np.uint32)
+    od = np.ascontiguousarray(outdeg, dtype=np.uint32) if outdeg is not None else None
+    _check(lib().asc_write_graph(path.encode(), fmt, len(ptr) - 1, int(ptr[-1]), ptr.ctypes.data,
+                                 edges.ctypes.data, od.ctypes.data if od is not None else None))
+
+
+def _opt(fn, path, *args, out_dtype=np.uint32, want_output=True):
+    V = int(np.fromfile(path, dtype=np.uint64, count=1)[0])
+    out = np.empty(V, out_dtype) if want_output else None
+    st = Stats()
+    _check(fn(path.encode(), *args, out.ctypes.data if out is not None else None, ctypes.byref(st)))
+    return out, st.as_dict()
+
+
+def bfs_opt(path, source, advise_rate=0.0):
+    return _opt(lib().asc_bfs_opt, path, source, advise_rate)
+
+
+def cc_opt(path, advise_rate=0.0):
+    return _opt(lib().asc_cc_opt, path, advise_rate)
+
+
+def sssp_opt(path, source, advise_rate=0.0):
+    return _opt(lib().asc_sssp_opt, path, source, advise_rate)
+
+
+def pr_opt(path, advise_rate=0.0):
+    return _opt(lib().asc_pr_opt, path, advise_rate, out_dtype=np.float64)

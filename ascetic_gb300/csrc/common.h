@@ -1,0 +1,97 @@
+// Internal declarations shared by the host code and the CUDA engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ascetic.h"
+
+namespace asc {
+
+// Thread-local last-error message (asc_last_error).
+void set_error(const char *fmt, ...);
+asc_status fail(asc_status s, const char *fmt, ...);
+asc_status cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define ASC_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t _asc_e = (call);                                                    \
+        if (_asc_e != cudaSuccess) return ::asc::cuda_fail(_asc_e, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define ASC_TRY(call)                                  \
+    do {                                               \
+        asc_status _asc_s = (call);                    \
+        if (_asc_s != ASC_OK) return _asc_s;           \
+    } while (0)
+
+// Engine tunables (block size is fixed at compile time, the rest per graph).
+constexpr int kBlock = 256;
+
+struct Tuning {
+    uint32_t huge_degree = 512;   // lists longer than this are cut into segments
+    uint32_t segment_edges = 2048;  // edges per segment work item
+    uint32_t ctas_per_sm = 4;     // persistent expansion grid = SMs x this
+};
+
+// Per-run device state, sized for one graph and reused across its runs.
+struct Workspace {
+    uint64_t V = 0;
+    uint32_t *val = nullptr;         // u32 values (BFS/SSSP/CC)
+    uint32_t *bitmap = nullptr;      // next-frontier membership, one bit per vertex
+    uint32_t *queue[2] = {nullptr, nullptr};   // [V]: static entries from 0, on-demand from S
+    uint64_t *segs[2] = {nullptr, nullptr};    // segment items (v << 32 | k)
+    uint64_t segcap_static = 0, segcap_ondemand = 0;
+    uint32_t *ctl = nullptr;         // device control block (counters, work cursors, stats)
+    uint32_t *h_ctl = nullptr;       // pinned mirror for per-iteration readback
+    // PageRank buffers (allocated on the first PR run)
+    void *pr_rank = nullptr;         // f64 or f32 [V]
+    void *pr_contrib[2] = {nullptr, nullptr};
+    void *pr_sum = nullptr;          // segment partial sums [V]
+    size_t pr_elem = 0;
+    uint32_t *huge_list = nullptr;   // vertices with degree > huge_degree, static first
+    uint32_t n_huge_static = 0, n_huge_total = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> phase_events;
+    Tuning tune;
+    int num_sms = 0;
+    uint64_t device_bytes = 0;
+};
+
+}  // namespace asc
+
+struct asc_graph {
+    uint64_t V = 0, E = 0;
+    uint32_t edge_words = 1;      // 1: u32 destination, 2: {dst, weight}
+    bool is_csc = false;
+    uint32_t max_degree = 0;
+    uint32_t max_weight = 0;
+    // host (pinned)
+    uint32_t *h_ptr = nullptr;    // V+1 offsets (u32: E < 2^32)
+    uint32_t *h_edges = nullptr;  // E * edge_words, mapped for device reads
+    uint32_t *h_outdeg = nullptr; // V (CSC graphs)
+    // device
+    const uint32_t *d_host_edges = nullptr;  // device address of h_edges (zero-copy reads)
+    uint32_t *d_ptr = nullptr;
+    uint32_t *d_static = nullptr;  // edge prefix [0, static_edges)
+    uint32_t *d_outdeg = nullptr;
+    uint64_t static_edges = 0;
+    uint32_t static_vertices = 0;  // S: vertices [0, S) have all edges in the prefix
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    asc::Workspace *ws = nullptr;
+    uint64_t device_vertex_bytes = 0;
+};
+
+namespace asc {
+// engine.cu
+asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
+                         asc_stats *st);
+asc_status run_pagerank(asc_graph *g, const asc_params &p, void *out, asc_stats *st);
+void free_workspace(asc_graph *g);
+// graph.cpp
+asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t param_size);
+}  // namespace asc

@@ -1,0 +1,213 @@
+/*
+ * ascetic.h: C ABI of the GB300-native out-of-GPU-memory graph iteration engine.
+ *
+ * The library (libascetic_gb300.so) keeps a static prefix of a graph's CSR edge
+ * array resident on the GPU and reads the edges of the active vertices that the
+ * prefix does not hold directly from pinned host memory over the host link
+ * (NVLink-C2C on GB300), compacting them per iteration on the device.
+ * BFS, SSSP, CC (min-label) and PageRank run as hand-written sm_103a kernels.
+ *
+ * Conventions
+ *  - Every call returns an asc_status; nothing calls exit(). asc_last_error()
+ *    gives the message of the last failure on the calling thread.
+ *  - The caller owns every output buffer; the library owns device memory and
+ *    frees it in asc_graph_close().
+ *  - One asc_graph may be used by one thread at a time.
+ *  - Value encoding follows the reference (GraphMeta.cuh:374-467): BFS level + 1,
+ *    SSSP distance + 1, unreached = V + 1, CC minimum label, PR as double (or
+ *    float when asked for).
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *  - ptgraph CLI flags --input/--type/--source/--adviseK  (main.cu:4-22,
+ *    ArgumentParser.cu:15-48): the ptgraph binary built from
+ *    ascetic_gb300/csrc/ptgraph.cpp, which calls only this header.
+ *  - void bfs_opt(string path, uint src, double adviseRate)  (CalculateOpt.cuh:11)
+ *  - void cc_opt(string path, double adviseRate)             (CalculateOpt.cuh:12)
+ *  - void sssp_opt(string path, uint src, double adviseRate) (CalculateOpt.cuh:13)
+ *  - void pr_opt(string path, double adviseRate)             (CalculateOpt.cuh:14)
+ *  - GraphMeta<EdgeType>::readDataFromFile / initGraphHost / initGraphDevice
+ *    (GraphMeta.cuh:151-297): asc_graph_open / asc_graph_from_csr.
+ */
+#ifndef ASCETIC_GB300_H
+#define ASCETIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum asc_status {
+    ASC_OK = 0,
+    ASC_ERR_INVALID = 1,      /* bad argument */
+    ASC_ERR_BAD_FILE = 2,     /* unreadable, short or malformed graph file */
+    ASC_ERR_BUDGET = 3,       /* the device budget or device memory cannot hold the run */
+    ASC_ERR_CUDA = 4,         /* CUDA runtime failure */
+    ASC_ERR_TIMEOUT = 5,      /* iteration limit or a bounded device wait ran out */
+    ASC_ERR_CANCELLED = 6,    /* a queued or running query was cancelled */
+    ASC_ERR_UNSUPPORTED = 7,  /* e.g. E >= 2^32, weights that could wrap u32, wrong file type */
+    ASC_ERR_NO_DEVICE = 8,    /* no usable CUDA device */
+    ASC_ERR_NOMEM = 9,        /* host allocation failed */
+    ASC_ERR_BUSY = 10         /* server queue full */
+} asc_status;
+
+typedef enum asc_format {
+    ASC_FMT_AUTO = 0,    /* detect from header and file size */
+    ASC_FMT_BCSR = 1,    /* u64 V, u64 E, u64 ptr[V], u32 col[E]                     (.bcsr) */
+    ASC_FMT_BWCSR = 2,   /* u64 V, u64 E, u64 ptr[V], {u32 dst, u32 w}[E]            (.bwcsr) */
+    ASC_FMT_BCSC = 3,    /* u64 V, u64 E, u32 outDeg[V], u64 ptr[V], u32 src[E]     (.bcsc) */
+    ASC_FMT_BCSR32 = 4   /* u32 V, u32 E, u32 ptr[V], u32 col[E] (legacy, bfs.cu:14-23) */
+} asc_format;
+
+typedef enum asc_algo { ASC_BFS = 0, ASC_SSSP = 1, ASC_CC = 2, ASC_PR = 3 } asc_algo;
+
+typedef enum asc_budget_mode {
+    ASC_BUDGET_ALL = 0,      /* whole edge array resident (no cap) */
+    ASC_BUDGET_FRAC = 1,     /* value = fraction of the edge-array bytes for the static region */
+    ASC_BUDGET_BYTES = 2,    /* value = bytes for the static region */
+    ASC_BUDGET_ADVISE_K = 3, /* value = reference --adviseK: fraction of free device memory left
+                                after the vertex arrays (GraphMeta.cuh:310-354); 0 = its auto formula */
+    ASC_BUDGET_EDGES = 4     /* value = exact static edge count (no fragment rounding) */
+} asc_budget_mode;
+
+typedef struct asc_budget {
+    uint32_t mode;           /* asc_budget_mode */
+    uint32_t fragment_edges; /* static prefix rounded down to a multiple of this (0 = 4096,
+                                the reference's fragment, GraphMeta.cuh:143,353-354) */
+    double value;
+} asc_budget;
+
+typedef struct asc_graph asc_graph;
+
+typedef struct asc_graph_info {
+    uint64_t vertices;
+    uint64_t edges;
+    uint32_t edge_bytes;          /* 4 (u32 destination) or 8 ({dst, weight}) */
+    uint32_t is_csc;              /* 1 for .bcsc (in-edges + out-degree block) */
+    uint64_t static_edges;        /* edges in the device-resident prefix */
+    uint64_t static_vertices;     /* vertices [0, static_vertices) have every edge in the prefix */
+    uint64_t device_edge_bytes;   /* static region bytes (what the budget caps) */
+    uint64_t device_vertex_bytes; /* offsets and per-run vertex state (outside the cap) */
+    uint64_t host_pinned_bytes;   /* pinned host copy of the edge array (on-demand source) */
+    uint32_t max_degree;
+    uint32_t max_weight;          /* 0 for unweighted graphs */
+} asc_graph_info;
+
+typedef enum asc_pr_mode {
+    ASC_PR_REF = 0,  /* reference PageRank: 0.15 + 0.85*sum, per-vertex stop at |delta| <= 0.001,
+                        FP64 (gpu_kernels.cuh:533-594) */
+    ASC_PR_STD = 1   /* standard PageRank: damping, (1-d)/V teleport, dangling mass spread uniformly,
+                        stop at FP64 L1 residual < tolerance or max_iterations */
+} asc_pr_mode;
+
+typedef enum asc_precision { ASC_F64 = 0, ASC_F32 = 1 } asc_precision;
+
+enum {
+    ASC_RUN_NO_OUTPUT = 1u << 0,   /* do not copy the values out (out may be NULL) */
+    ASC_RUN_DEVICE_OUT = 1u << 1,  /* out is a device pointer */
+    ASC_RUN_PHASE_TIMING = 1u << 2 /* time static and on-demand kernels separately (CUDA events) */
+};
+
+typedef struct asc_params {
+    uint32_t pr_mode;        /* asc_pr_mode (default ASC_PR_REF) */
+    uint32_t precision;      /* asc_precision of the PR ranks and sums (default ASC_F64);
+                                ASC_F32 keeps FP64 dangling and residual reductions */
+    double damping;          /* ASC_PR_STD (default 0.85) */
+    double tolerance;        /* ASC_PR_STD L1 stop (default 1e-9) */
+    int32_t max_iterations;  /* 0 = until convergence (PR std default 100) */
+    uint32_t flags;          /* ASC_RUN_* */
+} asc_params;
+
+typedef struct asc_stats {
+    int32_t iterations;
+    int32_t status_detail;
+    uint64_t frontier_vertices;  /* sum over iterations of processed frontier vertices */
+    uint64_t ondemand_vertices;  /* of which on-demand (edges read from host memory) */
+    uint64_t edges_processed;    /* sum over iterations of their degrees */
+    uint64_t ondemand_edges;     /* of which read from host memory (moved over the host link) */
+    uint64_t ondemand_bytes;     /* ondemand_edges x edge bytes */
+    uint64_t reached_vertices;   /* BFS/SSSP: value < V + 1 */
+    uint64_t reached_edges;      /* BFS/SSSP: sum of out-degrees of reached vertices (TEPS numerator) */
+    double ms_total;             /* device time from the first to the last kernel of the run */
+    double ms_static;            /* with ASC_RUN_PHASE_TIMING: static-region expansion kernels */
+    double ms_ondemand;          /* with ASC_RUN_PHASE_TIMING: on-demand expansion kernels */
+    double ms_copyout;           /* result copy to the caller's buffer */
+    double residual;             /* PR std: last FP64 L1 residual */
+    uint32_t kernel_launches;    /* kernels of this library launched by the run */
+    uint32_t reserved;
+} asc_stats;
+
+/* ---- status and errors -------------------------------------------------- */
+const char *asc_status_string(asc_status s);
+/* Copies the calling thread's last error message into buf; returns its length. */
+size_t asc_last_error(char *buf, size_t n);
+const char *asc_version(void);
+/* Number of usable CUDA devices (0 when none); never fails. */
+int asc_device_count(void);
+
+/* ---- graphs -------------------------------------------------------------- */
+void asc_budget_default(asc_budget *b);
+/* Reads a reference-format file into pinned host memory and uploads the static
+ * prefix chosen by the budget (replaces GraphMeta::readDataFromFile +
+ * initGraphHost + initGraphDevice, GraphMeta.cuh:151-297). */
+asc_status asc_graph_open(const char *path, asc_format fmt, const asc_budget *budget, asc_graph **out);
+/* Builds a graph from caller arrays (copied): ptr has V+1 entries (ptr[V] = E);
+ * edges holds E u32 destinations (edge_bytes 4) or E {dst, weight} pairs
+ * (edge_bytes 8); outdeg (V entries) marks a CSC graph for PageRank, else NULL. */
+asc_status asc_graph_from_csr(uint64_t V, uint64_t E, const uint64_t *ptr, const void *edges,
+                              uint32_t edge_bytes, const uint32_t *outdeg, const asc_budget *budget,
+                              asc_graph **out);
+asc_status asc_graph_info_get(const asc_graph *g, asc_graph_info *info);
+/* Releases every device and pinned buffer of the graph. NULL is ignored. */
+asc_status asc_graph_close(asc_graph *g);
+
+/* ---- runs ---------------------------------------------------------------- */
+void asc_params_default(asc_params *p);
+/* One query: BFS/SSSP from source, CC, or PR. out receives V values: uint32
+ * for BFS/SSSP/CC, double (or float with precision ASC_F32) for PR. params
+ * and stats may be NULL. */
+asc_status asc_run(asc_graph *g, asc_algo algo, uint32_t source, const asc_params *params, void *out,
+                   asc_stats *stats);
+
+/* Reference-shaped entry points (CalculateOpt.cuh:11-14): open the file with the
+ * reference's --adviseK budget rule, run, close. out (nullable) receives the
+ * values the reference keeps in valueD / valuePrD. */
+asc_status asc_bfs_opt(const char *path, uint32_t source, double advise_rate, uint32_t *out,
+                       asc_stats *stats);
+asc_status asc_cc_opt(const char *path, double advise_rate, uint32_t *out, asc_stats *stats);
+asc_status asc_sssp_opt(const char *path, uint32_t source, double advise_rate, uint32_t *out,
+                        asc_stats *stats);
+asc_status asc_pr_opt(const char *path, double advise_rate, double *out, asc_stats *stats);
+
+/* ---- synthetic graphs and files -------------------------------------------- */
+enum {
+    ASC_RMAT_WEIGHTS = 1u << 0,    /* emit {dst, weight} pairs, weight uniform in [wmin, wmax] */
+    ASC_RMAT_SYMMETRIC = 1u << 1,  /* append the reverse of every edge before sorting */
+    ASC_RMAT_TRANSPOSE = 1u << 2   /* emit the CSC (in-edge) arrays and the out-degrees */
+};
+/* Seeded RMAT edge list sorted by source into CSR (self-loops and duplicates
+ * kept, each list in generation order; reversed edges follow the originals).
+ * Deterministic for a seed on any host and thread count. Sizes: V = 2^scale,
+ * E = V * edge_factor (x2 with ASC_RMAT_SYMMETRIC). ptr receives V+1 entries,
+ * edges E u32 (or 2E with weights), outdeg V entries (ASC_RMAT_TRANSPOSE only). */
+asc_status asc_rmat_csr(uint32_t scale, uint32_t edge_factor, uint64_t seed, double a, double b, double c,
+                        uint32_t wmin, uint32_t wmax, uint32_t flags, uint64_t *ptr, void *edges,
+                        uint32_t *outdeg);
+/* Generates straight into a graph's pinned buffers (no extra host copy). */
+asc_status asc_graph_rmat(uint32_t scale, uint32_t edge_factor, uint64_t seed, double a, double b, double c,
+                          uint32_t wmin, uint32_t wmax, uint32_t flags, const asc_budget *budget,
+                          asc_graph **out);
+/* Host-link probe: best pinned host-to-device copy-engine bandwidth and best
+ * bandwidth of SM loads from mapped pinned host memory, in GB/s (1e9 B/s),
+ * over a buffer of the given size (measurement helper, no reference counterpart). */
+asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double *sm_read_gbs);
+
+/* Writes a graph file in a reference format from CSR arrays (ptr has V+1 entries). */
+asc_status asc_write_graph(const char *path, asc_format fmt, uint64_t V, uint64_t E, const uint64_t *ptr,
+                           const void *edges, const uint32_t *outdeg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,185 @@
+"""CUDA engine against the oracle and the reference golden vectors (GPU).
+
+Every value array is compared bit for bit (BFS, SSSP, CC) or within 1e-6
+max-abs per vertex (PageRank), across static/on-demand splits from
+all-on-demand to all-static, through the C ABI.
+"""
+import json
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import ascetic_gb300 as A
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+PR_TOL = 1e-6   # max-abs per vertex against the FP64 oracle
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine():
+    A.lib()
+    if A.device_count() == 0:
+        pytest.fail("no CUDA device: the engine has no CPU fallback")
+
+
+@pytest.mark.parametrize("graph", sorted(MANIFEST["graphs"]))
+def test_golden_vectors(graph):
+    """Same graph, same static prefix size as the reference run, same result."""
+    z = np.load(os.path.join(GOLDEN, graph + ".npz"))
+    cache = {}
+    for r in MANIFEST["graphs"][graph]["runs"]:
+        algo = r["algo"]
+        key = (algo, r["static_edges"])
+        if key not in cache:
+            b = A.make_budget(edges=r["static_edges"])
+            if algo in ("bfs",):
+                cache[key] = A.Graph.from_csr(z["ptr"], z["col"], budget=b)
+            elif algo == "sssp":
+                cache[key] = A.Graph.from_csr(z["ptr"], z["adj"], budget=b)
+            elif algo == "cc":
+                cache[key] = A.Graph.from_csr(z["sptr"], z["scol"], budget=b)
+            else:
+                cache[key] = A.Graph.from_csr(z["cptr"], z["ccol"], outdeg=z["outdeg"], budget=b)
+        g = cache[key]
+        exp = z[r["key"]]
+        if algo == "pr_ref":
+            got, _ = g.run("pr")
+            assert np.abs(got - exp).max() <= PR_TOL, r["key"]
+        else:
+            got, _ = g.run(algo, r["source"])
+            assert np.array_equal(got, exp), r["key"]
+    for g in cache.values():
+        g.close()
+
+
+FRACS = [1.0, 0.5, 0.25, 0.05, 0.0]
+
+
+@pytest.mark.parametrize("frac", FRACS)
+def test_bfs_matches_oracle(frac):
+    ptr, col = A.rmat_csr(14, 16, 11)
+    deg = np.diff(ptr)
+    srcs = [0, int(np.nonzero(deg)[0][-1]), int(np.nonzero(deg == 0)[0][0]) if (deg == 0).any() else 5]
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+        for s in srcs:
+            got, st = g.run("bfs", s)
+            exp = oracle.bfs(ptr, col, s)
+            assert np.array_equal(got, exp), (frac, s)
+            assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
+            if 0 < frac < 1 and st["reached_vertices"] > 1000:
+                assert st["ondemand_edges"] > 0
+
+
+@pytest.mark.parametrize("frac", FRACS)
+def test_sssp_matches_oracle(frac):
+    ptr, adj = A.rmat_csr(13, 16, 12, weights=(1, 63))
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=frac)) as g:
+        for s in (0, 77):
+            got, _ = g.run("sssp", s)
+            assert np.array_equal(got, oracle.sssp(ptr, adj, s)), (frac, s)
+
+
+@pytest.mark.parametrize("frac", FRACS)
+def test_cc_matches_oracle(frac):
+    ptr, col = A.rmat_csr(13, 8, 13, symmetric=True)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+        got, _ = g.run("cc")
+    assert np.array_equal(got, oracle.cc(ptr, col))
+
+
+def test_cc_directed_is_min_ancestor():
+    ptr, col = A.rmat_csr(12, 4, 14)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.3)) as g:
+        got, _ = g.run("cc")
+    assert np.array_equal(got, oracle.cc(ptr, col))
+
+
+@pytest.mark.parametrize("frac", [1.0, 0.3, 0.0])
+def test_pagerank_ref_and_std(frac):
+    cptr, ccol, od = A.rmat_csr(13, 16, 15, transpose=True)
+    with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=frac)) as g:
+        got, st = g.run("pr")
+        exp, it = oracle.pr_ref(cptr, ccol, od)
+        assert np.abs(got - exp).max() <= PR_TOL
+        for prec in (A.F64, A.F32):
+            got, st = g.run("pr", params=A.make_params(pr_mode=A.PR_STD, precision=prec))
+            exp, it, res = oracle.pr_std(cptr, ccol, od)
+            err = np.abs(got.astype(np.float64) - exp).max()
+            assert err <= PR_TOL, (prec, err)
+            if prec == A.F64:
+                assert st["iterations"] == it
+
+
+def test_huge_vertices_and_segments():
+    """A star whose hub list is far above the segment threshold, mostly on demand."""
+    V = 50000
+    src = np.concatenate([np.zeros(V - 1, np.int64), np.arange(1, V), [7] * 3000])
+    dst = np.concatenate([np.arange(1, V), np.zeros(V - 1, np.int64), np.arange(3000) + 100])
+    ptr, col = A.formats.csr_from_edges(V, src, dst)
+    for frac in (0.0, 0.02, 1.0):
+        with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+            for s in (0, 5, 7):
+                got, _ = g.run("bfs", s)
+                assert np.array_equal(got, oracle.bfs(ptr, col, s)), (frac, s)
+            got, _ = g.run("cc")
+            assert np.array_equal(got, oracle.cc(ptr, col))
+
+
+def test_file_formats_and_reference_entry_points():
+    ptr, col = A.rmat_csr(11, 8, 16)
+    _, adj = A.rmat_csr(11, 8, 16, weights=(1, 63))
+    cptr, ccol, od = A.rmat_csr(11, 8, 16, transpose=True)
+    d = tempfile.mkdtemp()
+    files = {"g.bcsr": (A.FMT_BCSR, ptr, col, None), "g.bwcsr": (A.FMT_BWCSR, ptr, adj, None),
+             "g.bcsc": (A.FMT_BCSC, cptr, ccol, od), "g.bcsr32": (A.FMT_BCSR32, ptr, col, None)}
+    for name, (fmt, p, e, o) in files.items():
+        A.write_graph(os.path.join(d, name), fmt, p, e, o)
+    got, st = A.bfs_opt(os.path.join(d, "g.bcsr"), 3, 0.5)
+    assert np.array_equal(got, oracle.bfs(ptr, col, 3))
+    got, _ = A.sssp_opt(os.path.join(d, "g.bwcsr"), 3, 0.0)
+    assert np.array_equal(got, oracle.sssp(ptr, adj, 3))
+    got, _ = A.cc_opt(os.path.join(d, "g.bcsr"))
+    assert np.array_equal(got, oracle.cc(ptr, col))
+    got, _ = A.pr_opt(os.path.join(d, "g.bcsc"))
+    assert np.abs(got - oracle.pr_ref(cptr, ccol, od)[0]).max() <= PR_TOL
+    with A.Graph.open(os.path.join(d, "g.bcsr32"), budget=A.make_budget(frac=0.25)) as g:
+        got, _ = g.run("bfs", 3)
+        assert np.array_equal(got, oracle.bfs(ptr, col, 3))
+
+
+def test_errors_are_statuses():
+    ptr, col = A.rmat_csr(8, 4, 17)
+    with A.Graph.from_csr(ptr, col) as g:
+        with pytest.raises(A.AscError) as e:
+            g.run("bfs", 1 << 20)
+        assert e.value.status == A.ERR_INVALID
+        with pytest.raises(A.AscError) as e:
+            g.run("sssp", 0)
+        assert e.value.status == A.ERR_UNSUPPORTED
+        with pytest.raises(A.AscError) as e:
+            g.run("pr")
+        assert e.value.status == A.ERR_UNSUPPORTED
+    bad = col.copy()
+    bad[5] = 1 << 20
+    with pytest.raises(A.AscError) as e:
+        A.Graph.from_csr(ptr, bad)
+    assert e.value.status == A.ERR_INVALID or e.value.status == A.ERR_BAD_FILE
+
+
+def test_single_vertex_and_isolated_source():
+    with A.Graph.from_csr(np.array([0, 1], np.uint64), np.array([0], np.uint32)) as g:
+        got, _ = g.run("bfs", 0)
+        assert got.tolist() == [1]
+        got, _ = g.run("cc")
+        assert got.tolist() == [0]
+    ptr, col = A.formats.csr_from_edges(10, np.array([1, 2]), np.array([2, 3]))
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.0)) as g:
+        got, st = g.run("bfs", 0)
+        assert got.tolist() == [1] + [11] * 9
+        assert st["reached_vertices"] == 1 and st["reached_edges"] == 0
