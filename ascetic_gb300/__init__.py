@@ -38,7 +38,8 @@ ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_count", "asc_budget_default",
             "asc_graph_open", "asc_graph_from_csr", "asc_graph_info_get", "asc_graph_close",
             "asc_params_default", "asc_run", "asc_bfs_opt", "asc_cc_opt", "asc_sssp_opt", "asc_pr_opt",
-            "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe"]
+            "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe",
+            "asc_bfs_device_noalloc"]
 
 
 class EngineUnavailable(RuntimeError):
@@ -124,6 +125,7 @@ def lib():
                            ctypes.c_int),
         "asc_write_graph": ([ctypes.c_char_p, ctypes.c_int, c_u64, c_u64, c_vp, c_vp, c_vp], ctypes.c_int),
         "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
+        "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

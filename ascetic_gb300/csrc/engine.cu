@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "common.h"
 
@@ -1026,4 +1027,160 @@ extern "C" asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_
     if (dma_h2d_gbs) *dma_h2d_gbs = best_dma;
     if (sm_read_gbs) *sm_read_gbs = best_sm;
     return st;
+}
+
+// ------------------------------------------------- allocation-free BFS -------
+//
+// asc_bfs_device_noalloc runs the same BFS expansion kernel over a CSR graph the
+// caller already holds in device memory, for callers that cannot allocate
+// device memory at query time: a process whose device memory is owned by
+// another allocator (a framework's caching pool sized to the whole GPU, where
+// a cudaMalloc of its own would fail or fragment the pool), or a latency-bound
+// loop where cudaMalloc/cudaFree (which can synchronize the device) are not
+// allowed. Its scratch state (frontier lists, segment lists, the next-frontier
+// bitmap, counters) lives in one file-scope device array of fixed size, which
+// every GPU that loads this library holds until the process exits.
+namespace asc {
+namespace {
+
+constexpr uint64_t kNoAllocMaxV = 1ull << 20;   // vertices
+constexpr uint64_t kNoAllocMaxE = 1ull << 24;   // edges
+constexpr uint32_t kNoAllocHuge = 512;          // same degree buckets as the default Tuning
+constexpr uint32_t kNoAllocSeg = 2048;
+// segment items never exceed E/seg_len (full segments) + E/huge (one partial per long list)
+constexpr uint64_t kNoAllocMaxSegs = kNoAllocMaxE / kNoAllocSeg + kNoAllocMaxE / kNoAllocHuge + 1;
+
+constexpr uint64_t na_round(uint64_t x) { return (x + 255) & ~255ull; }
+constexpr uint64_t kNaCtl = 0;
+constexpr uint64_t kNaBitmap = na_round(kNaCtl + 4 * CTL_WORDS);
+constexpr uint64_t kNaQueue0 = na_round(kNaBitmap + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaQueue1 = na_round(kNaQueue0 + 4 * kNoAllocMaxV);
+constexpr uint64_t kNaSegs0 = na_round(kNaQueue1 + 4 * kNoAllocMaxV);
+constexpr uint64_t kNaSegs1 = na_round(kNaSegs0 + 8 * kNoAllocMaxSegs);
+constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // about 9.2 MB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// In host code g_noalloc_scratch names a host-side stand-in, not device memory;
+// kernels get the device address looked up once per device.
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mutex;
+unsigned char *g_na_addr[kNaMaxDevices] = {nullptr};
+
+// Checks the caller's CSR on the device: offsets start at 0, never decrease,
+// end at E, destinations are < V. flag[0] becomes nonzero on the first defect.
+__global__ void noalloc_validate_kernel(const uint32_t *ptr, const uint32_t *col, uint32_t V, uint32_t E,
+                                        uint32_t *flag) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && (ptr[0] != 0 || ptr[V] != E)) atomicOr(flag, 1u);
+    for (uint32_t v = t; v < V; v += stride)
+        if (ptr[v] > ptr[v + 1]) atomicOr(flag, 2u);
+    for (uint32_t i = t; i < E; i += stride)
+        if (col[i] >= V) atomicOr(flag, 4u);
+}
+
+asc_status noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    ASC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNaMaxDevices) return fail(ASC_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_addr[dev]) {
+        void *p = nullptr;
+        ASC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_na_addr[dev] = (unsigned char *)p;
+    }
+    *out = g_na_addr[dev];
+    return ASC_OK;
+}
+
+}  // namespace
+}  // namespace asc
+
+extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint32_t *d_row_offsets,
+                                             const uint32_t *d_col, uint32_t source, uint32_t *d_levels,
+                                             void *stream) {
+    using namespace asc;
+    if (!d_row_offsets || !d_levels || (!d_col && E))
+        return fail(ASC_ERR_INVALID, "asc_bfs_device_noalloc: null device pointer");
+    if (V == 0 || V > kNoAllocMaxV)
+        return fail(ASC_ERR_BUDGET, "asc_bfs_device_noalloc: V = %llu outside [1, %llu], the fixed scratch limit",
+                    (unsigned long long)V, (unsigned long long)kNoAllocMaxV);
+    if (E > kNoAllocMaxE)
+        return fail(ASC_ERR_BUDGET, "asc_bfs_device_noalloc: E = %llu above %llu, the fixed scratch limit",
+                    (unsigned long long)E, (unsigned long long)kNoAllocMaxE);
+    if (source >= V) return fail(ASC_ERR_INVALID, "source %u is not a vertex (V = %llu)", source,
+                                 (unsigned long long)V);
+    unsigned char *base = nullptr;
+    ASC_TRY(noalloc_scratch(&base));
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t *ctl = (uint32_t *)(base + kNaCtl);
+    uint32_t *bitmap = (uint32_t *)(base + kNaBitmap);
+    uint32_t *queue[2] = {(uint32_t *)(base + kNaQueue0), (uint32_t *)(base + kNaQueue1)};
+    uint64_t *segs[2] = {(uint64_t *)(base + kNaSegs0), (uint64_t *)(base + kNaSegs1)};
+    const uint32_t V32 = (uint32_t)V, E32 = (uint32_t)E;
+    int dev = 0, sms = 0;
+    ASC_CUDA(cudaGetDevice(&dev));
+    ASC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint32_t fill = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((V + kBlock - 1) / kBlock, sms * 8ull));
+
+    // the array keeps the previous call's contents: clear the counters first
+    ASC_CUDA(cudaMemsetAsync(ctl, 0, 4 * CTL_WORDS, s));
+    noalloc_validate_kernel<<<fill, kBlock, 0, s>>>(d_row_offsets, d_col, V32, E32, ctl + CTL_PR);
+    ASC_CUDA(cudaGetLastError());
+    uint32_t flag = 0;
+    ASC_CUDA(cudaMemcpyAsync(&flag, ctl + CTL_PR, 4, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    if (flag)
+        return fail(ASC_ERR_INVALID, "asc_bfs_device_noalloc: malformed CSR (%s%s%s)",
+                    flag & 1 ? "offsets must start at 0 and end at E; " : "",
+                    flag & 2 ? "offsets decrease; " : "", flag & 4 ? "destination >= V" : "");
+
+    RegionArgs a;
+    memset(&a, 0, sizeof(a));
+    a.ptr = d_row_offsets;
+    a.edges = d_col;
+    a.val = d_levels;
+    a.bitmap = bitmap;
+    a.S = V32;  // the whole graph is device resident: one region
+    a.V = V32;
+    a.huge = kNoAllocHuge;
+    a.seg_len = kNoAllocSeg;
+    a.segcap_static = (uint32_t)kNoAllocMaxSegs;
+    a.stats = (unsigned long long *)(ctl + CTL_STATS);
+    // seed: the source lands in parity 0
+    a.cnt_out = ctl;
+    a.q_out = queue[0];
+    a.seg_out = segs[0];
+    init_values_kernel<kBFS><<<fill, kBlock, 0, s>>>(d_levels, V32, source);
+    seed_kernel<<<1, kBlock, 0, s>>>(a, source, 0);
+    ASC_CUDA(cudaGetLastError());
+    uint32_t cnt[4] = {0, 0, 0, 0};
+    ASC_CUDA(cudaMemcpyAsync(cnt, ctl, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    int parity = 0;
+    int64_t iters = 0;
+    while (cnt[0] | cnt[2]) {
+        if (++iters > (int64_t)V + 2) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %lld iterations",
+                                                  (long long)iters);
+        const int po = 1 - parity;
+        ASC_CUDA(cudaMemsetAsync(ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
+        ASC_CUDA(cudaMemsetAsync(bitmap, 0, 4 * (V / 32 + 2), s));
+        a.region = 0;
+        a.q_in = queue[parity];
+        a.seg_in = segs[parity];
+        a.cnt_in = ctl + CTL_BLOCK * parity;
+        a.cnt_out = ctl + CTL_BLOCK * po;
+        a.q_out = queue[po];
+        a.seg_out = segs[po];
+        a.work = a.cnt_out + 4;
+        const uint64_t items = (uint64_t)cnt[2] + (cnt[0] + kBlock - 1) / kBlock;
+        const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)sms * 4));
+        expand_kernel<kBFS, 1><<<grid, kBlock, 0, s>>>(a);
+        ASC_CUDA(cudaGetLastError());
+        ASC_CUDA(cudaMemcpyAsync(cnt, a.cnt_out, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        ASC_CUDA(cudaStreamSynchronize(s));
+        parity = po;
+    }
+    return ASC_OK;
 }

@@ -203,6 +203,31 @@ asc_status asc_graph_rmat(uint32_t scale, uint32_t edge_factor, uint64_t seed, d
  * over a buffer of the given size (measurement helper, no reference counterpart). */
 asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double *sm_read_gbs);
 
+/* ---- allocation-free BFS ------------------------------------------------- */
+/* BFS over a CSR graph that the caller already holds in device memory, for
+ * callers that cannot allocate device memory when they run a query: a process
+ * whose device memory belongs to another allocator (for example a framework's
+ * caching pool that reserved the whole GPU, where a cudaMalloc of our own would
+ * fail or fragment that pool), or a latency-bound loop where cudaMalloc and
+ * cudaFree, which may synchronize the device, are not allowed.
+ * No counterpart in the reference (whose drivers always allocate, GraphMeta.cuh:237-297).
+ *
+ * Inputs: d_row_offsets (V+1 u32, device), d_col (E u32, device); output:
+ * d_levels (V u32, device) in the reference encoding (level + 1, unreached V + 1).
+ * stream is a cudaStream_t (NULL = the default stream); the call returns after
+ * the BFS has finished on it.
+ * Limits: V <= 1,048,576 and E <= 16,777,216; larger graphs return
+ * ASC_ERR_BUDGET. The CSR is checked on the device first (ASC_ERR_INVALID).
+ * Scratch: one fixed device array of about 9.2 MB in this library, held by
+ * every GPU that loads it until the process exits; no cudaMalloc, cudaFree or
+ * allocating library routine is called. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current, so
+ * make that first call before any stream capture. All calls share the array
+ * (counters are cleared at the start of each call): calls that overlap on the
+ * GPU, on any stream or thread, race and must not be issued. */
+asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint32_t *d_row_offsets, const uint32_t *d_col,
+                                  uint32_t source, uint32_t *d_levels, void *stream);
+
 /* Writes a graph file in a reference format from CSR arrays (ptr has V+1 entries). */
 asc_status asc_write_graph(const char *path, asc_format fmt, uint64_t V, uint64_t E, const uint64_t *ptr,
                            const void *edges, const uint32_t *outdeg);
