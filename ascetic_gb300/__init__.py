@@ -30,7 +30,7 @@ BFS, SSSP, CC, PR = range(4)
 BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES = range(5)
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
-RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING = 1, 2, 4
+RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP = 1, 2, 4, 8
 RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 

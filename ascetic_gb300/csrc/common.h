@@ -56,6 +56,8 @@ struct Workspace {
     uint32_t n_huge_static = 0, n_huge_total = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> phase_events;
+    cudaGraphExec_t loop_exec[3] = {nullptr, nullptr, nullptr};  // BFS, SSSP, CC iteration loops
+    uint32_t loop_cap[3] = {0, 0, 0};
     Tuning tune;
     int num_sms = 0;
     uint64_t device_bytes = 0;

@@ -51,7 +51,10 @@ enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 // Stats at word 16 (u64): edges static, edges on-demand, frontier vertices
 // static, frontier vertices on-demand, reached vertices, reached edges. PageRank FP64 accumulators at word 32:
 // residual[2], dangling[2].
-enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_PR = 32, CTL_WORDS = 64 };
+// Word 28 counts iterations, word 29 flags an iteration cap hit and word 30
+// counts loop-body executions when the loop runs as a CUDA graph.
+enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_ITERS = 28, CTL_TIMEOUT = 29, CTL_BODIES = 30, CTL_PR = 32,
+       CTL_WORDS = 64 };
 
 struct RegionArgs {
     const uint32_t *ptr;
@@ -150,8 +153,7 @@ __device__ __forceinline__ void push_warp(const RegionArgs &a, bool won, uint32_
 }
 
 template <int ALG, int WORDS>
-__device__ __forceinline__ bool relax(const RegionArgs &a, uint32_t vu, uint64_t idx, uint32_t &v) {
-    uint32_t nv;
+__device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint64_t idx, uint32_t &v, uint32_t &nv) {
     if (WORDS == 2) {
         uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + idx);
         v = e.x;
@@ -160,14 +162,23 @@ __device__ __forceinline__ bool relax(const RegionArgs &a, uint32_t vu, uint64_t
         v = __ldg(a.edges + idx);
         nv = ALG == kBFS ? vu + 1 : vu;
     }
-    // values only decrease, so a stale read can only be larger: never a missed update
-    if (nv >= a.val[v]) return false;
+}
+
+// Lowers val[v] to nv; true when this thread also won v's next-frontier bit.
+// cur is an earlier read of val[v]: values only decrease, so a stale read is
+// larger and can only cost an extra atomic, never a missed update.
+__device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t nv, uint32_t cur) {
+    if (nv >= cur) return false;
     uint32_t old = atomicMin(&a.val[v], nv);
     if (nv >= old) return false;
     uint32_t bit = 1u << (v & 31);
-    uint32_t prev = atomicOr(&a.bitmap[v >> 5], bit);
-    return (prev & bit) == 0;
+    return (atomicOr(&a.bitmap[v >> 5], bit) & bit) == 0;
 }
+
+// Each thread handles kUnroll edges per pass: all column loads are issued
+// first, then all destination-value loads, then the updates, so a thread keeps
+// kUnroll independent reads in flight (on-demand column reads cross the host link).
+constexpr int kUnroll = 4;
 
 template <int ALG, int WORDS>
 __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, Smem &sm) {
@@ -187,60 +198,77 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, S
     sm.vu[threadIdx.x] = vu;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     __syncthreads();
-    for (uint32_t base = 0; base < total; base += kBlock) {
-        const uint32_t e = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (e < total) {
-            int lo = 0, hi = kBlock;
-            while (hi - lo > 1) {
-                int mid = (lo + hi) >> 1;
-                if (sm.pref[mid] <= e) lo = mid;
-                else hi = mid;
+    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t e = base + k * kBlock + threadIdx.x;
+            v[k] = 0;
+            nv[k] = 0xffffffffu;  // never lower than a value: no update
+            if (e < total) {
+                int lo = 0, hi = kBlock;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (sm.pref[mid] <= e) lo = mid;
+                    else hi = mid;
+                }
+                load_edge<ALG, WORDS>(a, sm.vu[lo], (uint64_t)sm.start[lo] + (e - sm.pref[lo]), v[k], nv[k]);
             }
-            uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
-            won = relax<ALG, WORDS>(a, sm.vu[lo], idx, v);
         }
-        push_warp(a, won, v);
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? a.val[v[k]] : 0;
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) push_warp(a, lower(a, v[k], nv[k], cur[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
-        uint32_t nv = a.q_in ? min(kBlock, n_in - tile * kBlock)
-                             : min((uint32_t)kBlock, a.dense_end - a.dense_begin - tile * kBlock);
-        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nv);
+        uint32_t nvx = a.q_in ? min(kBlock, n_in - tile * kBlock)
+                              : min((uint32_t)kBlock, a.dense_end - a.dense_begin - tile * kBlock);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nvx);
     }
     __syncthreads();
 }
 
 template <int ALG, int WORDS>
 __device__ void expand_segment(const RegionArgs &a, uint64_t item) {
-    const uint32_t u = (uint32_t)(item >> 32), k = (uint32_t)item;
+    const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
     const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
-    const uint64_t b = (uint64_t)b0 + (uint64_t)k * a.seg_len;
+    const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     const uint32_t vu = a.val[u];
-    for (uint32_t base = 0; base < n; base += kBlock) {
-        const uint32_t j = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (j < n) won = relax<ALG, WORDS>(a, vu, b + j, v);
-        push_warp(a, won, v);
+    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t j = base + k * kBlock + threadIdx.x;
+            v[k] = 0;
+            nv[k] = 0xffffffffu;
+            if (j < n) load_edge<ALG, WORDS>(a, vu, b + j, v[k], nv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? a.val[v[k]] : 0;
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) push_warp(a, lower(a, v[k], nv[k], cur[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
-        if (k == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+        if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
     }
+}
+
+__device__ __forceinline__ void region_items(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg, uint32_t &items) {
+    n_in = a.q_in ? a.cnt_in[a.region] : 0;
+    nseg = a.cnt_in[2 + a.region];
+    const uint32_t nvert = a.q_in ? n_in : a.dense_end - a.dense_begin;
+    items = nseg + (nvert + kBlock - 1) / kBlock;
 }
 
 template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
     __shared__ Smem sm;
-    const uint32_t n_in = a.q_in ? a.cnt_in[a.region] : 0;
-    const uint32_t nseg = a.cnt_in[2 + a.region];
-    const uint32_t nvert = a.q_in ? n_in : a.dense_end - a.dense_begin;
-    const uint32_t ntiles = (nvert + kBlock - 1) / kBlock;
-    const uint32_t total = nseg + ntiles;
+    uint32_t n_in, nseg, total;
+    region_items(a, n_in, nseg, total);
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(a.work, 1u);
         __syncthreads();
@@ -250,6 +278,65 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
         if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w]);
         else expand_tile<ALG, WORDS>(a, w - nseg, n_in, sm);
     }
+}
+
+// Both regions in one launch. Work items alternate between the on-demand and
+// the static region while both have items left, so every SM mixes HBM-bound
+// static work with link-bound on-demand work; on-demand segments and tiles
+// are handed out first within their region.
+struct FusedArgs {
+    RegionArgs r0, r1;
+    uint32_t *work;
+};
+
+template <int ALG, int WORDS>
+__global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
+    __shared__ Smem sm;
+    uint32_t n0, s0, i0, n1, s1, i1;
+    region_items(x.r0, n0, s0, i0);
+    region_items(x.r1, n1, s1, i1);
+    const uint32_t m = min(i0, i1), total = i0 + i1;
+    for (;;) {
+        if (threadIdx.x == 0) sm.work = atomicAdd(x.work, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        __syncthreads();
+        if (w >= total) break;
+        bool od;
+        uint32_t local;
+        if (w < 2 * m) {
+            od = (w & 1) == 0;
+            local = w >> 1;
+        } else {
+            od = i1 > i0;
+            local = m + (w - 2 * m);
+        }
+        if (od) {
+            if (local < s1) expand_segment<ALG, WORDS>(x.r1, x.r1.seg_in[local]);
+            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, sm);
+        } else {
+            if (local < s0) expand_segment<ALG, WORDS>(x.r0, x.r0.seg_in[local]);
+            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, sm);
+        }
+    }
+}
+
+// End of one CUDA-graph loop body (two iterations: parity 0 then parity 1).
+// Block 1 holds what the first half produced (the second half's input),
+// block 0 what the second half produced. Keeps looping while block 0 is
+// non-empty, counts the iterations that had input, and stops at the cap.
+__global__ void loop_cond_kernel(cudaGraphConditionalHandle h, uint32_t *ctl, uint32_t cap) {
+    const uint32_t *b0 = ctl, *b1 = ctl + CTL_BLOCK;
+    const bool second = (b1[0] | b1[1] | b1[2] | b1[3]) != 0;
+    bool more = (b0[0] | b0[1] | b0[2] | b0[3]) != 0;
+    const uint32_t it = ctl[CTL_ITERS] + 1 + (second ? 1 : 0);
+    ctl[CTL_ITERS] = it;
+    ctl[CTL_BODIES] += 1;
+    if (more && it >= cap) {
+        ctl[CTL_TIMEOUT] = 1;
+        more = false;
+    }
+    cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 template <int ALG>
@@ -562,6 +649,12 @@ asc_status ensure_workspace(asc_graph *g) {
     g->ws = ws;
     ws->V = g->V;
     ASC_CUDA(cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, g->device));
+    {
+        // persistent grids fill the GPU: as many CTAs per SM as stay resident
+        int per_sm = 0;
+        ASC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, expand_fused_kernel<kSSSP, 2>, kBlock, 0));
+        ws->tune.ctas_per_sm = (uint32_t)std::max(1, per_sm);
+    }
     const uint64_t V = g->V;
     const uint32_t S = g->static_vertices;
     const Tuning &t = ws->tune;
@@ -672,6 +765,18 @@ void launch_expand(asc_graph *g, const RegionArgs &a, uint32_t grid) {
 }
 
 typedef void (*ExpandFn)(asc_graph *, const RegionArgs &, uint32_t);
+typedef void (*FusedFn)(cudaStream_t, const FusedArgs &, uint32_t);
+
+template <int ALG, int WORDS>
+void launch_fused(cudaStream_t s, const FusedArgs &x, uint32_t grid) {
+    expand_fused_kernel<ALG, WORDS><<<grid, kBlock, 0, s>>>(x);
+}
+
+FusedFn pick_fused(asc_algo algo, uint32_t words) {
+    if (algo == ASC_BFS) return words == 2 ? launch_fused<kBFS, 2> : launch_fused<kBFS, 1>;
+    if (algo == ASC_CC) return words == 2 ? launch_fused<kCC, 2> : launch_fused<kCC, 1>;
+    return launch_fused<kSSSP, 2>;
+}
 
 ExpandFn pick_expand(asc_algo algo, uint32_t words) {
     if (algo == ASC_BFS) return words == 2 ? launch_expand<kBFS, 2> : launch_expand<kBFS, 1>;
@@ -713,6 +818,73 @@ struct PhaseTimer {
     }
 };
 
+// Builds the iteration loop of one algorithm as a CUDA graph: a conditional
+// WHILE node whose body runs two iterations (parity 0 then 1; an iteration
+// with an empty input costs only empty launches) and loop_cond_kernel. The
+// kernels read their frontier sizes from the control block, so nothing
+// returns to the host between iterations.
+asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
+    Workspace *ws = g->ws;
+    const int slot = algo == ASC_BFS ? 0 : (algo == ASC_SSSP ? 1 : 2);
+    if (ws->loop_exec[slot] && ws->loop_cap[slot] == cap) return ASC_OK;
+    if (ws->loop_exec[slot]) {
+        cudaGraphExecDestroy(ws->loop_exec[slot]);
+        ws->loop_exec[slot] = nullptr;
+    }
+    FusedFn fused = pick_fused(algo, g->edge_words);
+    const uint32_t V = (uint32_t)g->V;
+    const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    asc_status st = ASC_OK;
+    auto chk = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == ASC_OK) st = cuda_fail(e, what, __FILE__, __LINE__);
+        return st == ASC_OK;
+    };
+    cudaGraphConditionalHandle handle;
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node;
+    if (chk(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream") &&
+        chk(cudaGraphCreate(&graph, 0), "cudaGraphCreate") &&
+        chk(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault), "handle")) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (chk(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp), "cudaGraphAddNode")) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            if (chk(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "capture")) {
+                for (int parity = 0; parity < 2; parity++) {
+                    const int po = 1 - parity;
+                    cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, cs);
+                    cudaMemsetAsync(ws->bitmap, 0, 4 * (V / 32 + 2), cs);
+                    FusedArgs x;
+                    x.r0 = region_args(g, parity, 0, false);
+                    x.r1 = region_args(g, parity, 1, false);
+                    x.work = x.r0.cnt_out + 4;
+                    fused(cs, x, grid);
+                }
+                loop_cond_kernel<<<1, 1, 0, cs>>>(handle, ws->ctl, cap);
+                cudaGraph_t out = nullptr;
+                chk(cudaStreamEndCapture(cs, &out), "end capture");
+            }
+        }
+    }
+    if (st == ASC_OK) chk(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+    if (graph) cudaGraphDestroy(graph);
+    if (cs) cudaStreamDestroy(cs);
+    if (st != ASC_OK) {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGetLastError();
+        return st;
+    }
+    ws->loop_exec[slot] = exec;
+    ws->loop_cap[slot] = cap;
+    return ASC_OK;
+}
+
 }  // namespace
 
 void free_workspace(asc_graph *g) {
@@ -723,6 +895,8 @@ void free_workspace(asc_graph *g) {
                     ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
         if (p) cudaFree(p);
     if (ws->h_ctl) cudaFreeHost(ws->h_ctl);
+    for (auto &e : ws->loop_exec)
+        if (e) cudaGraphExecDestroy(e);
     for (auto e : ws->ev)
         if (e) cudaEventDestroy(e);
     for (auto e : ws->phase_events) cudaEventDestroy(e);
@@ -740,6 +914,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     uint32_t launches = 0;
     PhaseTimer pt(ws, (p.flags & ASC_RUN_PHASE_TIMING) != 0);
     ExpandFn expand = pick_expand(algo, g->edge_words);
+    FusedFn fused = pick_fused(algo, g->edge_words);
 
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
@@ -753,29 +928,50 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     seed_kernel<<<all ? fill_grid(ws, V) : 1, kBlock, 0, s>>>(sa, source, all ? 1 : 0);
     launches += 2;
     ASC_CUDA(cudaGetLastError());
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
-    ASC_CUDA(cudaStreamSynchronize(s));
-
-    int parity = 0;
-    int iters = 0;
     const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
-    uint32_t cnt[4];
-    memcpy(cnt, ws->h_ctl, sizeof(cnt));
+    const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP));
+    int iters = 0;
     double phase_ms[2] = {0, 0};
+    if (use_graph) {
+        const uint32_t gcap = (uint32_t)std::min<int64_t>(cap, 0x7fffffff);
+        ASC_TRY(build_loop_graph(g, algo, gcap));
+        const int slot = algo == ASC_BFS ? 0 : (algo == ASC_SSSP ? 1 : 2);
+        ASC_CUDA(cudaGraphLaunch(ws->loop_exec[slot], s));
+        launches += 1;
+    }
+    uint32_t cnt[4] = {0, 0, 0, 0};
+    if (!use_graph) {
+        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
+        ASC_CUDA(cudaStreamSynchronize(s));
+        memcpy(cnt, ws->h_ctl, sizeof(cnt));
+    }
+    int parity = 0;
     while (cnt[0] | cnt[1] | cnt[2] | cnt[3]) {
         if (iters >= cap) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
         iters++;
         const int po = 1 - parity;
         ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
         ASC_CUDA(cudaMemsetAsync(ws->bitmap, 0, 4 * (V / 32 + 2), s));
-        for (int region = 0; region < 2; region++) {
-            const uint64_t items = (uint64_t)cnt[2 + region] + (cnt[region] + kBlock - 1) / kBlock;
-            if (!items) continue;
-            RegionArgs a = region_args(g, parity, region, false);
-            ASC_TRY(pt.begin(region));
-            pt.record(s);
-            expand(g, a, grid_for(ws, items));
-            pt.record(s);
+        if (pt.on) {
+            // diagnostic: one launch per region, each timed on its own
+            for (int region = 0; region < 2; region++) {
+                const uint64_t items = (uint64_t)cnt[2 + region] + (cnt[region] + kBlock - 1) / kBlock;
+                if (!items) continue;
+                RegionArgs a = region_args(g, parity, region, false);
+                ASC_TRY(pt.begin(region));
+                pt.record(s);
+                expand(g, a, grid_for(ws, items));
+                pt.record(s);
+                launches++;
+            }
+        } else {
+            const uint64_t items = (uint64_t)cnt[2] + (cnt[0] + kBlock - 1) / kBlock + (uint64_t)cnt[3] +
+                                   (cnt[1] + kBlock - 1) / kBlock;
+            FusedArgs x;
+            x.r0 = region_args(g, parity, 0, false);
+            x.r1 = region_args(g, parity, 1, false);
+            x.work = x.r0.cnt_out + 4;
+            fused(s, x, grid_for(ws, items));
             launches++;
         }
         ASC_CUDA(cudaGetLastError());
@@ -798,8 +994,14 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
                                  s));
     }
     ASC_CUDA(cudaEventRecord(ws->ev[2], s));
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 6, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 4 * (CTL_BODIES + 1 - CTL_STATS),
+                             cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
+    if (use_graph) {
+        iters = (int)ws->h_ctl[CTL_ITERS];
+        launches += 3 * ws->h_ctl[CTL_BODIES] - 1;  // two expansions and the loop test per body
+        if (ws->h_ctl[CTL_TIMEOUT]) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
+    }
     if (st) {
         memset(st, 0, sizeof(*st));
         const unsigned long long *hs = (const unsigned long long *)(ws->h_ctl + CTL_STATS);
@@ -965,9 +1167,16 @@ asc_status run_pagerank(asc_graph *g, const asc_params &p, void *out, asc_stats 
 
 namespace {
 __global__ void link_read_kernel(const uint4 *__restrict__ src, size_t n16, unsigned long long *sink) {
+    // four independent 16-byte loads in flight per thread
     uint32_t acc = 0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        uint4 a = __ldg(src + i), b = __ldg(src + i + stride), c = __ldg(src + i + 2 * stride),
+              d = __ldg(src + i + 3 * stride);
+        acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+    }
+    for (; i < n16; i += stride) {
         uint4 v = __ldg(src + i);
         acc ^= v.x ^ v.y ^ v.z ^ v.w;
     }
@@ -999,9 +1208,15 @@ extern "C" asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_
         chk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr")) {
         memset(h, 1, bytes);
         for (int i = 0; i < iters + 1 && st == ASC_OK; i++) {
+            // one copy per quarter, issued back to back on one stream
             float ms = 0;
             chk(cudaEventRecord(e0, s), "rec");
-            chk(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s), "memcpy");
+            const uint64_t q = (bytes / 4) & ~(uint64_t)15;
+            for (int k = 0; k < 4; k++) {
+                uint64_t off = k * q, n = k == 3 ? bytes - off : q;
+                chk(cudaMemcpyAsync((char *)d + off, (const char *)h + off, n, cudaMemcpyHostToDevice, s),
+                    "memcpy");
+            }
             chk(cudaEventRecord(e1, s), "rec");
             chk(cudaEventSynchronize(e1), "sync");
             chk(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
@@ -1010,7 +1225,7 @@ extern "C" asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_
         for (int i = 0; i < iters + 1 && st == ASC_OK; i++) {
             float ms = 0;
             chk(cudaEventRecord(e0, s), "rec");
-            link_read_kernel<<<sms * 8, 256, 0, s>>>((const uint4 *)hd, bytes / 16, sink);
+            link_read_kernel<<<sms * 16, 256, 0, s>>>((const uint4 *)hd, bytes / 16, sink);
             chk(cudaGetLastError(), "launch");
             chk(cudaEventRecord(e1, s), "rec");
             chk(cudaEventSynchronize(e1), "sync");

@@ -106,7 +106,10 @@ typedef enum asc_precision { ASC_F64 = 0, ASC_F32 = 1 } asc_precision;
 enum {
     ASC_RUN_NO_OUTPUT = 1u << 0,   /* do not copy the values out (out may be NULL) */
     ASC_RUN_DEVICE_OUT = 1u << 1,  /* out is a device pointer */
-    ASC_RUN_PHASE_TIMING = 1u << 2 /* time static and on-demand kernels separately (CUDA events) */
+    ASC_RUN_PHASE_TIMING = 1u << 2, /* time static and on-demand kernels separately (CUDA events);
+                                       implies a host-driven iteration loop */
+    ASC_RUN_HOST_LOOP = 1u << 3     /* drive iterations from the host (one readback per iteration)
+                                       instead of the CUDA-graph loop */
 };
 
 typedef struct asc_params {

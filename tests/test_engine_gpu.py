@@ -59,6 +59,9 @@ def test_golden_vectors(graph):
 
 
 FRACS = [1.0, 0.5, 0.25, 0.05, 0.0]
+# the iteration loop runs as a CUDA graph by default; the host-driven loop and
+# the per-region timed launches must give the same values
+LOOPS = [0, A.RUN_HOST_LOOP, A.RUN_PHASE_TIMING]
 
 
 @pytest.mark.parametrize("frac", FRACS)
@@ -68,12 +71,17 @@ def test_bfs_matches_oracle(frac):
     srcs = [0, int(np.nonzero(deg)[0][-1]), int(np.nonzero(deg == 0)[0][0]) if (deg == 0).any() else 5]
     with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
         for s in srcs:
-            got, st = g.run("bfs", s)
             exp = oracle.bfs(ptr, col, s)
-            assert np.array_equal(got, exp), (frac, s)
-            assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
-            if 0 < frac < 1 and st["reached_vertices"] > 1000:
-                assert st["ondemand_edges"] > 0
+            iters = set()
+            for flags in LOOPS:
+                got, st = g.run("bfs", s, params=A.make_params(flags=flags))
+                assert np.array_equal(got, exp), (frac, s, flags)
+                assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
+                if 0 < frac < 1 and st["reached_vertices"] > 1000:
+                    assert st["ondemand_edges"] > 0
+                iters.add(st["iterations"])
+            # BFS runs one level per iteration whatever drives the loop
+            assert len(iters) == 1
 
 
 @pytest.mark.parametrize("frac", FRACS)
@@ -81,16 +89,20 @@ def test_sssp_matches_oracle(frac):
     ptr, adj = A.rmat_csr(13, 16, 12, weights=(1, 63))
     with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=frac)) as g:
         for s in (0, 77):
-            got, _ = g.run("sssp", s)
-            assert np.array_equal(got, oracle.sssp(ptr, adj, s)), (frac, s)
+            exp = oracle.sssp(ptr, adj, s)
+            for flags in LOOPS:
+                got, _ = g.run("sssp", s, params=A.make_params(flags=flags))
+                assert np.array_equal(got, exp), (frac, s, flags)
 
 
 @pytest.mark.parametrize("frac", FRACS)
 def test_cc_matches_oracle(frac):
     ptr, col = A.rmat_csr(13, 8, 13, symmetric=True)
+    exp = oracle.cc(ptr, col)
     with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
-        got, _ = g.run("cc")
-    assert np.array_equal(got, oracle.cc(ptr, col))
+        for flags in LOOPS:
+            got, _ = g.run("cc", params=A.make_params(flags=flags))
+            assert np.array_equal(got, exp), flags
 
 
 def test_cc_directed_is_min_ancestor():
@@ -170,6 +182,19 @@ def test_errors_are_statuses():
     with pytest.raises(A.AscError) as e:
         A.Graph.from_csr(ptr, bad)
     assert e.value.status == A.ERR_INVALID or e.value.status == A.ERR_BAD_FILE
+
+
+def test_iteration_cap_returns_timeout():
+    V = 2000
+    s = np.arange(V - 1)
+    ptr, col = A.formats.csr_from_edges(V, s, s + 1)   # a chain: V-1 levels
+    with A.Graph.from_csr(ptr, col) as g:
+        for flags in (0, A.RUN_HOST_LOOP):
+            with pytest.raises(A.AscError) as e:
+                g.run("bfs", 0, params=A.make_params(max_iterations=10, flags=flags))
+            assert e.value.status == A.ERR_TIMEOUT
+            got, st = g.run("bfs", 0, params=A.make_params(flags=flags))
+            assert got[-1] == V and st["iterations"] == V
 
 
 def test_single_vertex_and_isolated_source():
