@@ -39,7 +39,7 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_graph_open", "asc_graph_from_csr", "asc_graph_info_get", "asc_graph_close",
             "asc_params_default", "asc_run", "asc_bfs_opt", "asc_cc_opt", "asc_sssp_opt", "asc_pr_opt",
             "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe",
-            "asc_bfs_device_noalloc"]
+            "asc_bfs_device_noalloc", "asc_run_batch"]
 
 
 class EngineUnavailable(RuntimeError):
@@ -126,6 +126,7 @@ def lib():
         "asc_write_graph": ([ctypes.c_char_p, ctypes.c_int, c_u64, c_u64, c_vp, c_vp, c_vp], ctypes.c_int),
         "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
         "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
+        "asc_run_batch": ([c_vp, ctypes.c_int, c_vp, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -260,6 +261,25 @@ class Graph:
         _check(lib().asc_run(self._h, algo, source, ctypes.byref(p),
                              out.ctypes.data if out is not None else None, ctypes.byref(st)))
         return out, st.as_dict()
+
+
+def _run_batch(self, algo, sources, params=None, out=None, no_output=False):
+    """Runs up to 64 BFS/SSSP sources together; returns ((n, V) values, stats)."""
+    if isinstance(algo, str):
+        algo = ALGOS[algo]
+    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    p = params if params is not None else make_params()
+    if no_output:
+        p.flags |= RUN_NO_OUTPUT
+    if out is None and not no_output:
+        out = np.empty((len(src), self.V), np.uint32)
+    st = Stats()
+    _check(lib().asc_run_batch(self._h, algo, src.ctypes.data, len(src), ctypes.byref(p),
+                               out.ctypes.data if out is not None else None, ctypes.byref(st)))
+    return out, st.as_dict()
+
+
+Graph.run_batch = _run_batch
 
 
 def rmat_csr(scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19, weights=None, symmetric=False,

@@ -131,6 +131,20 @@ asc_status asc_run(asc_graph *g, asc_algo algo, uint32_t source, const asc_param
     return run_traversal(g, algo, source, p, out, stats);
 }
 
+asc_status asc_run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n,
+                         const asc_params *params, void *out, asc_stats *stats) {
+    if (!g || !sources) return fail(ASC_ERR_INVALID, "asc_run_batch: graph and sources are required");
+    if (n == 0 || n > 64) return fail(ASC_ERR_INVALID, "asc_run_batch: %u sources, the batch holds 1 to 64", n);
+    if (algo != ASC_BFS && algo != ASC_SSSP)
+        return fail(ASC_ERR_UNSUPPORTED, "asc_run_batch runs BFS or SSSP sources");
+    asc_params p;
+    if (params) p = *params;
+    else asc_params_default(&p);
+    if (!out && !(p.flags & ASC_RUN_NO_OUTPUT)) return fail(ASC_ERR_INVALID, "asc_run_batch: out is NULL");
+    for (uint32_t i = 0; i < n; i++) ASC_TRY(check_algo(g, algo, sources[i]));
+    return run_batch(g, algo, sources, n, p, out, stats);
+}
+
 static asc_status opt_common(const char *path, asc_format fmt, double advise, asc_algo algo, uint32_t source,
                              void *out, asc_stats *stats) {
     asc_budget b;

@@ -35,13 +35,15 @@ struct Tuning {
     uint32_t huge_degree = 512;   // lists longer than this are cut into segments
     uint32_t segment_edges = 2048;  // edges per segment work item
     uint32_t ctas_per_sm = 4;     // persistent expansion grid = SMs x this
+    uint32_t dense_div = 64;      // walk a region in id order (frontier bitmap) when its list
+                                  // holds more than 1/dense_div of the region's vertices; 0 = never
 };
 
 // Per-run device state, sized for one graph and reused across its runs.
 struct Workspace {
     uint64_t V = 0;
     uint32_t *val = nullptr;         // u32 values (BFS/SSSP/CC)
-    uint32_t *bitmap = nullptr;      // next-frontier membership, one bit per vertex
+    uint32_t *bitmap[2] = {nullptr, nullptr};  // frontier membership by parity, one bit per vertex
     uint32_t *queue[2] = {nullptr, nullptr};   // [V]: static entries from 0, on-demand from S
     uint64_t *segs[2] = {nullptr, nullptr};    // segment items (v << 32 | k)
     uint64_t segcap_static = 0, segcap_ondemand = 0;
@@ -56,6 +58,12 @@ struct Workspace {
     uint32_t n_huge_static = 0, n_huge_total = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> phase_events;
+    // multi-source batches (up to 64 sources of one graph)
+    unsigned long long *ms_visit = nullptr, *ms_front = nullptr, *ms_next = nullptr;  // u64 [V]
+    uint32_t *ms_touched = nullptr;  // vertices whose next mask went non-zero this iteration [V]
+    uint32_t *ms_out = nullptr;      // per-source values, [n][V] (or vertex-major [V][64] distances)
+    uint32_t *ms_dist = nullptr;     // batched SSSP distances, vertex-major [V][64]
+    uint32_t ms_out_n = 0;
     cudaGraphExec_t loop_exec[3] = {nullptr, nullptr, nullptr};  // BFS, SSSP, CC iteration loops
     uint32_t loop_cap[3] = {0, 0, 0};
     Tuning tune;
@@ -93,6 +101,8 @@ namespace asc {
 asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
                          asc_stats *st);
 asc_status run_pagerank(asc_graph *g, const asc_params &p, void *out, asc_stats *st);
+asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params &p,
+                     void *out, asc_stats *st);
 void free_workspace(asc_graph *g);
 // graph.cpp
 asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t param_size);

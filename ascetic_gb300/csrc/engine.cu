@@ -60,7 +60,8 @@ struct RegionArgs {
     const uint32_t *ptr;
     const uint32_t *edges;        // region edge base, indexed by global edge offset
     uint32_t *val;
-    uint32_t *bitmap;
+    uint32_t *bitmap;             // next-frontier bitmap (written)
+    const uint32_t *bitmap_in;    // this iteration's frontier bitmap (null: no id-order mode)
     const uint32_t *q_in;         // this region's input list (null: dense range)
     const uint64_t *seg_in;       // this region's input segments
     const uint32_t *cnt_in;       // counts of the input frontier
@@ -76,7 +77,13 @@ struct RegionArgs {
     uint32_t seg_len;
     uint32_t segcap_static;
     uint32_t V;
+    uint32_t dense_div;
 };
+
+// How a tile picks its vertices: from the frontier list, every vertex of a
+// range, or the vertices of a range whose frontier bit is set (id order, so
+// the lists of neighbouring active vertices are read as one contiguous run).
+enum TileMode { kList = 0, kRange = 1, kBitmap = 2 };
 
 struct Smem {
     uint32_t pref[kBlock + 1];
@@ -181,14 +188,27 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
 constexpr int kUnroll = 4;
 
 template <int ALG, int WORDS>
-__device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, Smem &sm) {
+__device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, Smem &sm) {
     const uint32_t i = tile * kBlock + threadIdx.x;
+    bool act;
+    uint32_t u;
+    if (mode == kList) {
+        act = i < n_in;
+        u = act ? a.q_in[i] : 0;
+    } else {
+        u = a.dense_begin + i;
+        act = u < a.dense_end;
+        if (act && mode == kBitmap) act = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
+    }
+    if (mode == kBitmap && !__syncthreads_or(act)) return;  // no active vertex in this id range
     uint32_t deg = 0, start = 0, vu = 0;
-    if (a.q_in ? i < n_in : a.dense_begin + i < a.dense_end) {
-        uint32_t u = a.q_in ? a.q_in[i] : a.dense_begin + i;
+    if (act) {
         start = a.ptr[u];
         deg = a.ptr[u + 1] - start;
-        if (deg > a.huge) deg = 0;  // dense ranges: long lists are handled as segments
+        if (deg > a.huge) {
+            deg = 0;  // long lists are handled as segments
+            act = false;
+        }
         vu = a.val[u];
     }
     uint32_t total;
@@ -197,7 +217,7 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, S
     sm.start[threadIdx.x] = start;
     sm.vu[threadIdx.x] = vu;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
-    __syncthreads();
+    const uint32_t nact = __syncthreads_count(act);
     for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
         uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
 #pragma unroll
@@ -222,9 +242,7 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, S
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
-        uint32_t nvx = a.q_in ? min(kBlock, n_in - tile * kBlock)
-                              : min((uint32_t)kBlock, a.dense_end - a.dense_begin - tile * kBlock);
-        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nvx);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nact);
     }
     __syncthreads();
 }
@@ -257,10 +275,15 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item) {
     }
 }
 
-__device__ __forceinline__ void region_items(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg, uint32_t &items) {
+__device__ __forceinline__ void region_items(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg, uint32_t &items,
+                                             int &mode) {
     n_in = a.q_in ? a.cnt_in[a.region] : 0;
     nseg = a.cnt_in[2 + a.region];
-    const uint32_t nvert = a.q_in ? n_in : a.dense_end - a.dense_begin;
+    const uint32_t range = a.dense_end - a.dense_begin;
+    if (!a.q_in) mode = kRange;
+    else if (a.bitmap_in && a.dense_div && n_in > range / a.dense_div) mode = kBitmap;
+    else mode = kList;
+    const uint32_t nvert = mode == kList ? n_in : range;
     items = nseg + (nvert + kBlock - 1) / kBlock;
 }
 
@@ -268,7 +291,8 @@ template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
     __shared__ Smem sm;
     uint32_t n_in, nseg, total;
-    region_items(a, n_in, nseg, total);
+    int mode;
+    region_items(a, n_in, nseg, total, mode);
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(a.work, 1u);
         __syncthreads();
@@ -276,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
         __syncthreads();
         if (w >= total) break;
         if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w]);
-        else expand_tile<ALG, WORDS>(a, w - nseg, n_in, sm);
+        else expand_tile<ALG, WORDS>(a, w - nseg, n_in, mode, sm);
     }
 }
 
@@ -293,8 +317,9 @@ template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
     __shared__ Smem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
-    region_items(x.r0, n0, s0, i0);
-    region_items(x.r1, n1, s1, i1);
+    int m0, m1;
+    region_items(x.r0, n0, s0, i0, m0);
+    region_items(x.r1, n1, s1, i1, m1);
     const uint32_t m = min(i0, i1), total = i0 + i1;
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(x.work, 1u);
@@ -313,10 +338,10 @@ __global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
         }
         if (od) {
             if (local < s1) expand_segment<ALG, WORDS>(x.r1, x.r1.seg_in[local]);
-            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, sm);
+            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, m1, sm);
         } else {
             if (local < s0) expand_segment<ALG, WORDS>(x.r0, x.r0.seg_in[local]);
-            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, sm);
+            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, m0, sm);
         }
     }
 }
@@ -352,7 +377,9 @@ __global__ void seed_kernel(RegionArgs a, uint32_t src, uint32_t all) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool won = i < n;
-        push_warp(a, won, all ? i : src);
+        const uint32_t v = all ? i : src;
+        if (won) atomicOr(&a.bitmap[v >> 5], 1u << (v & 31));
+        push_warp(a, won, v);
     }
 }
 
@@ -680,7 +707,7 @@ asc_status ensure_workspace(asc_graph *g) {
         return ASC_OK;
     };
     ASC_TRY(dalloc((void **)&ws->val, 4 * V));
-    ASC_TRY(dalloc((void **)&ws->bitmap, 4 * (V / 32 + 2)));
+    for (int i = 0; i < 2; i++) ASC_TRY(dalloc((void **)&ws->bitmap[i], 4 * (V / 32 + 2)));
     for (int i = 0; i < 2; i++) {
         ASC_TRY(dalloc((void **)&ws->queue[i], 4 * V));
         ASC_TRY(dalloc((void **)&ws->segs[i], 8 * (cs + co)));
@@ -717,7 +744,9 @@ RegionArgs base_args(asc_graph *g, int parity_in) {
     memset(&a, 0, sizeof(a));
     a.ptr = g->d_ptr;
     a.val = ws->val;
-    a.bitmap = ws->bitmap;
+    a.bitmap = ws->bitmap[1 - parity_in];
+    a.bitmap_in = ws->bitmap[parity_in];
+    a.dense_div = ws->tune.dense_div;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
     a.huge = ws->tune.huge_degree;
@@ -737,10 +766,10 @@ RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
     RegionArgs a = base_args(g, parity_in);
     a.region = region;
     a.edges = region == 0 ? g->d_static : g->d_host_edges;
+    a.dense_begin = region == 0 ? 0 : g->static_vertices;
+    a.dense_end = region == 0 ? g->static_vertices : (uint32_t)g->V;
     if (dense) {
         a.q_in = nullptr;
-        a.dense_begin = region == 0 ? 0 : g->static_vertices;
-        a.dense_end = region == 0 ? g->static_vertices : (uint32_t)g->V;
     } else {
         a.q_in = ws->queue[parity_in] + (region == 0 ? 0 : g->static_vertices);
     }
@@ -859,7 +888,7 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
                 for (int parity = 0; parity < 2; parity++) {
                     const int po = 1 - parity;
                     cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, cs);
-                    cudaMemsetAsync(ws->bitmap, 0, 4 * (V / 32 + 2), cs);
+                    cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), cs);
                     FusedArgs x;
                     x.r0 = region_args(g, parity, 0, false);
                     x.r1 = region_args(g, parity, 1, false);
@@ -890,7 +919,11 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 void free_workspace(asc_graph *g) {
     Workspace *ws = g->ws;
     if (!ws) return;
-    for (void *p : {(void *)ws->val, (void *)ws->bitmap, (void *)ws->queue[0], (void *)ws->queue[1],
+    for (void *p : {(void *)ws->ms_visit, (void *)ws->ms_front, (void *)ws->ms_next, (void *)ws->ms_touched,
+                    (void *)ws->ms_out, (void *)ws->ms_dist})
+        if (p) cudaFree(p);
+    for (void *p : {(void *)ws->val, (void *)ws->bitmap[0], (void *)ws->bitmap[1], (void *)ws->queue[0],
+                    (void *)ws->queue[1],
                     (void *)ws->segs[0], (void *)ws->segs[1], (void *)ws->ctl, (void *)ws->huge_list, ws->pr_rank,
                     ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
         if (p) cudaFree(p);
@@ -918,7 +951,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
 
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
-    ASC_CUDA(cudaMemsetAsync(ws->bitmap, 0, 4 * (V / 32 + 2), s));
+    for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(ws->bitmap[i], 0, 4 * (V / 32 + 2), s));
     const uint32_t ig = fill_grid(ws, V);
     if (algo == ASC_CC) init_values_kernel<kCC><<<ig, kBlock, 0, s>>>(ws->val, V, 0);
     else if (algo == ASC_BFS) init_values_kernel<kBFS><<<ig, kBlock, 0, s>>>(ws->val, V, source);
@@ -951,7 +984,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         iters++;
         const int po = 1 - parity;
         ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
-        ASC_CUDA(cudaMemsetAsync(ws->bitmap, 0, 4 * (V / 32 + 2), s));
+        ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
         if (pt.on) {
             // diagnostic: one launch per region, each timed on its own
             for (int region = 0; region < 2; region++) {
@@ -1151,6 +1184,475 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         st->ms_copyout = ms;
         st->ms_static = phase_ms[0];
         st->ms_ondemand = phase_ms[1];
+        st->kernel_launches = launches;
+    }
+    return ASC_OK;
+}
+
+// -------------------------------------------- multi-source batches (<= 64) --
+//
+// Up to 64 BFS or SSSP queries of one graph advance together: each vertex
+// carries a 64-bit mask of the sources for which it is in the frontier, so one
+// read of an edge serves every source of the batch. BFS keeps 64-bit visited /
+// frontier / next masks per vertex and is level-synchronous, so each source's
+// levels equal a single-source BFS from it. Batched SSSP keeps a vertex-major
+// [V][64] distance block (one 256-byte row per vertex) and relaxes the sources
+// of a frontier vertex's mask lane by lane; its fixpoint per source is the
+// single-source one. The frontier lists, segments and the static/on-demand
+// split are the single-query engine's.
+namespace {
+
+constexpr int kMaxBatch = 64;
+
+struct MsArgs {
+    RegionArgs r0, r1;            // frontier lists/segments of both regions (val unused)
+    unsigned long long *visit;    // BFS: sources that reached v
+    unsigned long long *front;    // sources for which v is in the current frontier
+    unsigned long long *next;     // sources that reached v in this iteration (atomicOr)
+    uint32_t *touched;            // vertices whose next mask went non-zero
+    uint32_t *touched_cnt;
+    uint32_t *work;
+    uint32_t *dist;               // SSSP: [V][64]
+    uint32_t *levels;             // BFS: [n][V]
+    uint32_t n;                   // sources in the batch
+    uint32_t V;
+};
+
+struct MsSmem {
+    uint32_t pref[kBlock + 1];
+    uint32_t start[kBlock];
+    unsigned long long f[kBlock];
+    uint32_t warp[kWarps + 1];
+    uint32_t work;
+};
+
+__device__ __forceinline__ void push_touched(const MsArgs &m, bool won, uint32_t v) {
+    const unsigned msk = __ballot_sync(kFull, won);
+    if (!msk) return;
+    const int lane = threadIdx.x & 31, l = __ffs(msk) - 1;
+    uint32_t base = 0;
+    if (lane == l) base = atomicAdd(m.touched_cnt, (uint32_t)__popc(msk));
+    base = __shfl_sync(kFull, base, l);
+    if (won) m.touched[base + __popc(msk & ((1u << lane) - 1u))] = v;
+}
+
+// BFS relaxation of one edge for a whole mask: true when v's next mask was empty.
+__device__ __forceinline__ bool ms_reach(const MsArgs &m, uint32_t v, unsigned long long f,
+                                         unsigned long long vis) {
+    const unsigned long long nb = f & ~vis;
+    if (!nb) return false;
+    return atomicOr(&m.next[v], nb) == 0ull;
+}
+
+template <int WORDS>
+__device__ void ms_tile(const MsArgs &m, const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, MsSmem &sm) {
+    const uint32_t i = tile * kBlock + threadIdx.x;
+    bool act;
+    uint32_t u;
+    if (mode == kList) {
+        act = i < n_in;
+        u = act ? a.q_in[i] : 0;
+    } else {
+        u = a.dense_begin + i;
+        act = u < a.dense_end;
+        if (act && mode == kBitmap) act = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
+    }
+    if (mode == kBitmap && !__syncthreads_or(act)) return;
+    uint32_t deg = 0, start = 0;
+    unsigned long long f = 0;
+    if (act) {
+        start = a.ptr[u];
+        deg = a.ptr[u + 1] - start;
+        if (deg > a.huge) {
+            deg = 0;
+            act = false;
+        }
+        f = m.front[u];
+    }
+    uint32_t total;
+    uint32_t excl = block_excl_scan(deg, total, sm.warp);
+    sm.pref[threadIdx.x] = excl;
+    sm.start[threadIdx.x] = start;
+    sm.f[threadIdx.x] = f;
+    if (threadIdx.x == 0) sm.pref[kBlock] = total;
+    const uint32_t nact = __syncthreads_count(act);
+    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll];
+        unsigned long long fk[kUnroll], vis[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t e = base + k * kBlock + threadIdx.x;
+            v[k] = 0;
+            fk[k] = 0;
+            if (e < total) {
+                int lo = 0, hi = kBlock;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (sm.pref[mid] <= e) lo = mid;
+                    else hi = mid;
+                }
+                const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx);
+                fk[k] = sm.f[lo];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) vis[k] = fk[k] ? m.visit[v[k]] : ~0ull;
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) push_touched(m, ms_reach(m, v[k], fk[k], vis[k]), v[k]);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.stats[a.region], (unsigned long long)total);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nact);
+    }
+    __syncthreads();
+}
+
+template <int WORDS>
+__device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) {
+    const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+    const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
+    const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
+    const uint64_t e = min((uint64_t)e0, b + a.seg_len);
+    const uint32_t n = (uint32_t)(e - b);
+    const unsigned long long f = m.front[u];
+    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll];
+        unsigned long long vis[kUnroll];
+        bool ok[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t j = base + k * kBlock + threadIdx.x;
+            ok[k] = j < n;
+            v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j)) : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) push_touched(m, ok[k] && ms_reach(m, v[k], f, vis[k]), v[k]);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.stats[a.region], (unsigned long long)n);
+        if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+    }
+}
+
+template <int WORDS>
+__global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
+    __shared__ MsSmem sm;
+    uint32_t n0, s0, i0, n1, s1, i1;
+    int m0, m1;
+    region_items(m.r0, n0, s0, i0, m0);
+    region_items(m.r1, n1, s1, i1, m1);
+    const uint32_t mm = min(i0, i1), total = i0 + i1;
+    for (;;) {
+        if (threadIdx.x == 0) sm.work = atomicAdd(m.work, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        __syncthreads();
+        if (w >= total) break;
+        bool od;
+        uint32_t local;
+        if (w < 2 * mm) {
+            od = (w & 1) == 0;
+            local = w >> 1;
+        } else {
+            od = i1 > i0;
+            local = mm + (w - 2 * mm);
+        }
+        if (od) {
+            if (local < s1) ms_segment<WORDS>(m, m.r1, m.r1.seg_in[local]);
+            else ms_tile<WORDS>(m, m.r1, local - s1, n1, m1, sm);
+        } else {
+            if (local < s0) ms_segment<WORDS>(m, m.r0, m.r0.seg_in[local]);
+            else ms_tile<WORDS>(m, m.r0, local - s0, n0, m0, sm);
+        }
+    }
+}
+
+// After the expansion: the new sources of each touched vertex become its
+// frontier mask, BFS levels are written, and the vertex joins the next lists.
+template <bool BFS>
+__global__ void ms_apply_kernel(MsArgs m, uint32_t level) {
+    const uint32_t n = *m.touched_cnt;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool won = false;
+        uint32_t v = 0;
+        if (i < n) {
+            v = m.touched[i];
+            unsigned long long nb = m.next[v];
+            m.next[v] = 0;
+            if (BFS) {
+                nb &= ~m.visit[v];
+                m.visit[v] |= nb;
+                unsigned long long t = nb;
+                while (t) {
+                    const int s = __ffsll((long long)t) - 1;
+                    t &= t - 1;
+                    m.levels[(uint64_t)s * m.V + v] = level;
+                }
+            }
+            m.front[v] = nb;
+            won = nb != 0;
+            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
+        }
+        push_warp(m.r0, won, v);
+    }
+}
+
+__global__ void ms_init_kernel(MsArgs m, const uint32_t *sources, uint32_t fill, uint32_t sssp) {
+    const uint64_t total = sssp ? (uint64_t)m.V * kMaxBatch : (uint64_t)m.n * m.V;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        if (sssp) m.dist[i] = fill;
+        else m.levels[i] = fill;
+    }
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m.V; v += stride) {
+        if (!sssp) m.visit[v] = 0;
+        m.front[v] = 0;
+        m.next[v] = 0;
+    }
+}
+
+// Marks each source in its vertex's masks (duplicates share one frontier
+// entry) and pushes the distinct source vertices into the first frontier.
+__global__ void ms_seed_kernel(MsArgs m, const uint32_t *sources, uint32_t sssp) {
+    for (uint32_t base = 0; base < kMaxBatch; base += 32) {
+        const uint32_t i = base + threadIdx.x;
+        bool won = false;
+        uint32_t v = 0;
+        if (i < m.n) {
+            v = sources[i];
+            const unsigned long long bit = 1ull << i;
+            if (sssp) m.dist[(uint64_t)v * kMaxBatch + i] = 1;
+            else {
+                atomicOr(&m.visit[v], bit);
+                m.levels[(uint64_t)i * m.V + v] = 1;
+            }
+            won = atomicOr(&m.front[v], bit) == 0ull;
+            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
+        }
+        push_warp(m.r0, won, v);
+    }
+}
+
+// Batched SSSP expansion: one warp per work item (a frontier vertex, or one
+// segment of a long list); lanes are sources (two 32-source halves). Edges are
+// loaded 32 at a time, coalesced, and broadcast with shuffles; the 64
+// distances of a destination are one 256-byte row.
+__device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs &a, uint32_t u, uint64_t b,
+                                              uint32_t n) {
+    const int lane = threadIdx.x & 31;
+    const unsigned long long f = m.front[u];
+    const bool lo_on = (f >> lane) & 1ull, hi_on = (f >> (lane + 32)) & 1ull;
+    const uint32_t d_lo = lo_on ? m.dist[(uint64_t)u * kMaxBatch + lane] : 0;
+    const uint32_t d_hi = hi_on ? m.dist[(uint64_t)u * kMaxBatch + lane + 32] : 0;
+    const bool any_hi = (f >> 32) != 0;
+    for (uint32_t c = 0; c < n; c += 32) {
+        uint32_t ev = 0, ew = 0;
+        if (c + lane < n) {
+            const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
+            ev = e.x;
+            ew = e.y;
+        }
+        const uint32_t cn = min(32u, n - c);
+        for (uint32_t j = 0; j < cn; j++) {
+            const uint32_t v = __shfl_sync(kFull, ev, j);
+            const uint32_t w = __shfl_sync(kFull, ew, j);
+            uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+            bool imp_lo = false, imp_hi = false;
+            if (lo_on) {
+                const uint32_t nd = d_lo + w;
+                if (nd < row[lane]) imp_lo = nd < atomicMin(&row[lane], nd);
+            }
+            if (any_hi && hi_on) {
+                const uint32_t nd = d_hi + w;
+                if (nd < row[lane + 32]) imp_hi = nd < atomicMin(&row[lane + 32], nd);
+            }
+            const unsigned blo = __ballot_sync(kFull, imp_lo), bhi = __ballot_sync(kFull, imp_hi);
+            if (blo | bhi) {
+                bool won = false;
+                if (lane == 0) won = atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull;
+                push_touched(m, won, v);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t s, uint32_t local) {
+    const int lane = threadIdx.x & 31;
+    if (local < s) {
+        const uint64_t item = a.seg_in[local];
+        const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+        const uint64_t b = (uint64_t)a.ptr[u] + (uint64_t)k0 * a.seg_len;
+        const uint64_t e = min((uint64_t)a.ptr[u + 1], b + a.seg_len);
+        ms_sssp_edges(m, a, u, b, (uint32_t)(e - b));
+        if (lane == 0) {
+            atomicAdd(&a.stats[a.region], (unsigned long long)(e - b));
+            if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+        }
+    } else {
+        const uint32_t u = a.q_in[local - s];
+        const uint32_t b = a.ptr[u], e = a.ptr[u + 1];
+        ms_sssp_edges(m, a, u, b, e - b);
+        if (lane == 0) {
+            atomicAdd(&a.stats[a.region], (unsigned long long)(e - b));
+            atomicAdd(&a.stats[2 + a.region], 1ull);
+        }
+    }
+}
+
+// Work items are per warp and handed out 8 at a time: [static segments and
+// list vertices][on-demand segments and list vertices].
+__global__ void __launch_bounds__(kBlock) ms_sssp_expand_kernel(MsArgs m) {
+    const uint32_t n0 = m.r0.cnt_in[0], s0 = m.r0.cnt_in[2];
+    const uint32_t n1 = m.r1.cnt_in[1], s1 = m.r1.cnt_in[3];
+    const uint32_t t0 = s0 + n0, total = t0 + s1 + n1;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(m.work, 1u);
+        c = __shfl_sync(kFull, c, 0);
+        const uint32_t w0 = c * 8;
+        if (w0 >= total) break;
+        const uint32_t w1 = min(total, w0 + 8);
+        for (uint32_t w = w0; w < w1; w++) {
+            if (w < t0) ms_sssp_item(m, m.r0, s0, w);
+            else ms_sssp_item(m, m.r1, s1, w - t0);
+        }
+    }
+}
+
+// [V][64] distances -> [n][V] per-source rows (32x32 tiles through shared memory).
+__global__ void ms_transpose_kernel(const uint32_t *dist, uint32_t *out, uint32_t V, uint32_t n) {
+    __shared__ uint32_t t[32][33];
+    const uint32_t v0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+    for (uint32_t r = threadIdx.y; r < 32; r += blockDim.y) {
+        const uint32_t v = v0 + r, s = s0 + threadIdx.x;
+        t[r][threadIdx.x] = v < V ? dist[(uint64_t)v * kMaxBatch + s] : 0;
+    }
+    __syncthreads();
+    for (uint32_t r = threadIdx.y; r < 32; r += blockDim.y) {
+        const uint32_t s = s0 + r, v = v0 + threadIdx.x;
+        if (s < n && v < V) out[(uint64_t)s * V + v] = t[threadIdx.x][r];
+    }
+}
+
+}  // namespace
+
+asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params &p,
+                     void *out, asc_stats *st) {
+    ASC_TRY(ensure_workspace(g));
+    Workspace *ws = g->ws;
+    const uint32_t V = (uint32_t)g->V;
+    const bool sssp = algo == ASC_SSSP;
+    cudaStream_t s = g->stream;
+    if (!ws->ms_visit) {
+        ASC_CUDA(cudaMalloc(&ws->ms_visit, 8ull * V));
+        ASC_CUDA(cudaMalloc(&ws->ms_front, 8ull * V));
+        ASC_CUDA(cudaMalloc(&ws->ms_next, 8ull * V));
+        ASC_CUDA(cudaMalloc(&ws->ms_touched, 4ull * V));
+        ws->device_bytes += 28ull * V;
+    }
+    if (sssp && !ws->ms_dist) {
+        ASC_CUDA(cudaMalloc(&ws->ms_dist, 4ull * V * kMaxBatch));
+        ws->device_bytes += 4ull * V * kMaxBatch;
+    }
+    if (ws->ms_out_n < n) {
+        if (ws->ms_out) {
+            cudaFree(ws->ms_out);
+            ws->device_bytes -= 4ull * V * ws->ms_out_n;
+        }
+        ws->ms_out = nullptr;
+        ws->ms_out_n = 0;
+        ASC_CUDA(cudaMalloc(&ws->ms_out, 4ull * V * n));
+        ws->ms_out_n = n;
+        ws->device_bytes += 4ull * V * n;
+    }
+    uint32_t *d_src = ws->queue[1];  // the sources ride in the parity-1 list, unused until iteration 1
+    MsArgs m;
+    memset(&m, 0, sizeof(m));
+    m.visit = ws->ms_visit;
+    m.front = ws->ms_front;
+    m.next = ws->ms_next;
+    m.touched = ws->ms_touched;
+    m.dist = ws->ms_dist;
+    m.levels = ws->ms_out;
+    m.n = n;
+    m.V = V;
+    uint32_t launches = 0;
+
+    ASC_CUDA(cudaEventRecord(ws->ev[0], s));
+    ASC_CUDA(cudaMemcpyAsync(d_src, sources, 4ull * n, cudaMemcpyHostToDevice, s));
+    ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
+    for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(ws->bitmap[i], 0, 4 * (V / 32 + 2), s));
+    ms_init_kernel<<<fill_grid(ws, (uint64_t)V * (sssp ? kMaxBatch : n)), kBlock, 0, s>>>(m, d_src, V + 1,
+                                                                                           sssp ? 1 : 0);
+    m.r0 = base_args(g, 1);  // seeds land in parity 0
+    ms_seed_kernel<<<1, 32, 0, s>>>(m, d_src, sssp ? 1 : 0);
+    launches += 2;
+    ASC_CUDA(cudaGetLastError());
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 16, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    uint32_t cnt[4];
+    memcpy(cnt, ws->h_ctl, sizeof(cnt));
+    int parity = 0, iters = 0;
+    const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
+    uint32_t *touched_cnt = ws->ctl + CTL_PR;  // word 32: free outside PageRank
+    const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
+    while (cnt[0] | cnt[1] | cnt[2] | cnt[3]) {
+        if (iters >= cap) return fail(ASC_ERR_TIMEOUT, "batch has no fixpoint after %d iterations", iters);
+        iters++;
+        const int po = 1 - parity;
+        ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
+        ASC_CUDA(cudaMemsetAsync(touched_cnt, 0, 4, s));
+        ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
+        m.r0 = region_args(g, parity, 0, false);
+        m.r1 = region_args(g, parity, 1, false);
+        m.work = m.r0.cnt_out + 4;
+        m.touched_cnt = touched_cnt;
+        if (sssp) ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
+        else if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
+        else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
+        if (sssp) ms_apply_kernel<false><<<grid, kBlock, 0, s>>>(m, 0);
+        else ms_apply_kernel<true><<<grid, kBlock, 0, s>>>(m, (uint32_t)iters + 1);
+        launches += 2;
+        ASC_CUDA(cudaGetLastError());
+        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 16, cudaMemcpyDeviceToHost, s));
+        ASC_CUDA(cudaStreamSynchronize(s));
+        memcpy(cnt, ws->h_ctl, sizeof(cnt));
+        parity = po;
+    }
+    if (sssp) {
+        dim3 tg((V + 31) / 32, (n + 31) / 32);
+        ms_transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(ws->ms_dist, ws->ms_out, V, n);
+        launches++;
+    }
+    ASC_CUDA(cudaEventRecord(ws->ev[1], s));
+    ASC_CUDA(cudaGetLastError());
+    if (out && !(p.flags & ASC_RUN_NO_OUTPUT))
+        ASC_CUDA(cudaMemcpyAsync(out, ws->ms_out, 4ull * V * n,
+                                 (p.flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 s));
+    ASC_CUDA(cudaEventRecord(ws->ev[2], s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 6, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        const unsigned long long *hs = (const unsigned long long *)(ws->h_ctl + CTL_STATS);
+        st->iterations = iters;
+        st->edges_processed = hs[0] + hs[1];
+        st->ondemand_edges = hs[1];
+        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->frontier_vertices = hs[2] + hs[3];
+        st->ondemand_vertices = hs[3];
+        float ms = 0;
+        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[0], ws->ev[1]));
+        st->ms_total = ms;
+        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[1], ws->ev[2]));
+        st->ms_copyout = ms;
         st->kernel_launches = launches;
     }
     return ASC_OK;

@@ -173,6 +173,14 @@ void asc_params_default(asc_params *p);
 asc_status asc_run(asc_graph *g, asc_algo algo, uint32_t source, const asc_params *params, void *out,
                    asc_stats *stats);
 
+/* Up to 64 BFS or SSSP sources of one graph in one batch: every edge read
+ * serves all sources (64-bit per-vertex source masks). out receives n rows of
+ * V uint32 values, row i for sources[i], each identical to asc_run from that
+ * source. Duplicate sources are allowed. No reference counterpart (the
+ * reference runs one source per bfs_opt / sssp_opt call). */
+asc_status asc_run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params *params,
+                         void *out, asc_stats *stats);
+
 /* Reference-shaped entry points (CalculateOpt.cuh:11-14): open the file with the
  * reference's --adviseK budget rule, run, close. out (nullable) receives the
  * values the reference keeps in valueD / valuePrD. */

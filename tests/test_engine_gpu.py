@@ -105,6 +105,32 @@ def test_cc_matches_oracle(frac):
             assert np.array_equal(got, exp), flags
 
 
+@pytest.mark.parametrize("frac", [1.0, 0.25, 0.0])
+def test_batch_bfs_rows_equal_single_source(frac):
+    ptr, col = A.rmat_csr(13, 16, 31)
+    deg = np.diff(ptr)
+    rng = np.random.default_rng(5)
+    srcs = rng.choice(np.nonzero(deg)[0], size=62, replace=False).tolist() + [0, 0]   # duplicates allowed
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+        got, st = g.run_batch("bfs", srcs)
+        for i, s in enumerate(srcs):
+            assert np.array_equal(got[i], oracle.bfs(ptr, col, s)), (frac, i, s)
+        one, _ = g.run_batch("bfs", [srcs[3]])
+        assert np.array_equal(one[0], got[3])
+
+
+@pytest.mark.parametrize("frac", [1.0, 0.25, 0.0])
+def test_batch_sssp_rows_equal_single_source(frac):
+    ptr, adj = A.rmat_csr(12, 16, 32, weights=(1, 63))
+    deg = np.diff(ptr)
+    rng = np.random.default_rng(6)
+    srcs = rng.choice(np.nonzero(deg)[0], size=40, replace=False).tolist() + [7, 7, int(np.nonzero(deg == 0)[0][0])]
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=frac)) as g:
+        got, st = g.run_batch("sssp", srcs)
+        for i, s in enumerate(srcs):
+            assert np.array_equal(got[i], oracle.sssp(ptr, adj, s)), (frac, i, s)
+
+
 def test_cc_directed_is_min_ancestor():
     ptr, col = A.rmat_csr(12, 4, 14)
     with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.3)) as g:
