@@ -50,9 +50,7 @@ static asc_status check_algo(asc_graph *g, asc_algo algo, uint32_t source) {
         case ASC_CC:
             if (g->is_csc) return fail(ASC_ERR_UNSUPPORTED, "CC pushes along out-edges; this graph is bcsc");
             return ASC_OK;
-        case ASC_PR:
-            if (!g->is_csc)
-                return fail(ASC_ERR_UNSUPPORTED, "PageRank pulls over in-edges and needs out-degrees (bcsc)");
+        case ASC_PR:  // pull over in-edges (bcsc) or scatter over out-edges (bcsr / bwcsr)
             return ASC_OK;
     }
     return fail(ASC_ERR_INVALID, "unknown algorithm %d", (int)algo);

@@ -1658,8 +1658,327 @@ asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint3
     return ASC_OK;
 }
 
+// ------------------------------------------------- PageRank over CSR graphs --
+//
+// Graphs stored by out-edges (.bcsr / .bwcsr) run PageRank by scatter: every
+// vertex adds rank/outDeg to each out-neighbour's sum with an atomic add (FP32
+// or FP64 as asked), then one dense pass applies the update. The reference
+// PageRank semantics (per-vertex deactivation at |delta| <= 0.001, Jacobi
+// order) and the standard ones are the same as the pull kernels'; only the
+// summation order differs, as with any parallel sum.
+namespace {
+
+template <typename T>
+struct PushArgs {
+    RegionArgs r0, r1;         // dense ranges and the fixed segment list
+    const uint32_t *ptr;
+    T *rank;
+    const T *c_old;
+    T *c_new;
+    T *sum;
+    uint32_t *active;          // reference mode: one bit per still-active vertex
+    uint32_t *active_count;
+    double damping;
+    const double *dangling_prev;
+    double *acc;
+    uint32_t *work;
+};
+
+template <typename T>
+struct PushSmem {
+    uint32_t pref[kBlock + 1];
+    uint32_t start[kBlock];
+    T c[kBlock];
+    uint32_t warp[kWarps + 1];
+    uint32_t work;
+};
+
+template <typename T, int WORDS>
+__device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t tile, PushSmem<T> &sm) {
+    const uint32_t u = a.dense_begin + tile * kBlock + threadIdx.x;
+    uint32_t deg = 0, start = 0;
+    T c = (T)0;
+    if (u < a.dense_end) {
+        start = a.ptr[u];
+        deg = a.ptr[u + 1] - start;
+        if (deg > a.huge) deg = 0;
+        c = p.c_old[u];
+    }
+    uint32_t total;
+    const uint32_t excl = block_excl_scan(deg, total, sm.warp);
+    sm.pref[threadIdx.x] = excl;
+    sm.start[threadIdx.x] = start;
+    sm.c[threadIdx.x] = c;
+    if (threadIdx.x == 0) sm.pref[kBlock] = total;
+    __syncthreads();
+    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll];
+        T ck[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t e = base + k * kBlock + threadIdx.x;
+            v[k] = 0xffffffffu;
+            ck[k] = (T)0;
+            if (e < total) {
+                int lo = 0, hi = kBlock;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (sm.pref[mid] <= e) lo = mid;
+                    else hi = mid;
+                }
+                const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx);
+                ck[k] = sm.c[lo];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++)
+            if (v[k] != 0xffffffffu) atomicAdd(&p.sum[v[k]], ck[k]);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.stats[a.region], (unsigned long long)total);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)min((uint32_t)kBlock, a.dense_end - a.dense_begin -
+                                                                                       tile * kBlock));
+    }
+    __syncthreads();
+}
+
+template <typename T, int WORDS>
+__device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t item) {
+    const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+    const uint64_t b = (uint64_t)a.ptr[u] + (uint64_t)k0 * a.seg_len;
+    const uint64_t e = min((uint64_t)a.ptr[u + 1], b + a.seg_len);
+    const uint32_t n = (uint32_t)(e - b);
+    const T c = p.c_old[u];
+    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
+        uint32_t v[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const uint32_t j = base + k * kBlock + threadIdx.x;
+            v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j)) : 0xffffffffu;
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++)
+            if (v[k] != 0xffffffffu) atomicAdd(&p.sum[v[k]], c);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.stats[a.region], (unsigned long long)n);
+        if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+    }
+}
+
+template <typename T, int WORDS>
+__global__ void __launch_bounds__(kBlock) pr_scatter_kernel(PushArgs<T> p) {
+    __shared__ PushSmem<T> sm;
+    const uint32_t s0 = p.r0.cnt_in[2], s1 = p.r1.cnt_in[3];
+    const uint32_t t0 = s0 + (p.r0.dense_end - p.r0.dense_begin + kBlock - 1) / kBlock;
+    const uint32_t t1 = s1 + (p.r1.dense_end - p.r1.dense_begin + kBlock - 1) / kBlock;
+    const uint32_t mm = min(t0, t1), total = t0 + t1;
+    for (;;) {
+        if (threadIdx.x == 0) sm.work = atomicAdd(p.work, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        __syncthreads();
+        if (w >= total) break;
+        bool od;
+        uint32_t local;
+        if (w < 2 * mm) {
+            od = (w & 1) == 0;
+            local = w >> 1;
+        } else {
+            od = t1 > t0;
+            local = mm + (w - 2 * mm);
+        }
+        const RegionArgs &a = od ? p.r1 : p.r0;
+        const uint32_t s = od ? s1 : s0;
+        if (local < s) push_segment<T, WORDS>(p, a, a.seg_in[local]);
+        else push_tile<T, WORDS>(p, a, local - s, sm);
+    }
+}
+
+template <typename T, bool REF>
+__global__ void pr_push_apply_kernel(PushArgs<T> p, uint32_t V) {
+    __shared__ double red[2 * kWarps];
+    double res = 0, dang = 0;
+    uint32_t nact = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < V; base += stride) {
+        const uint32_t v = base + threadIdx.x;
+        if (v >= V) continue;
+        const T s = p.sum[v];
+        p.sum[v] = (T)0;
+        const uint32_t od = p.ptr[v + 1] - p.ptr[v];
+        if (REF) {
+            const uint32_t bit = 1u << (v & 31);
+            if (!(p.active[v >> 5] & bit)) {
+                p.c_new[v] = p.c_old[v];
+                continue;
+            }
+            const double r = (double)p.rank[v];
+            const double t = fma(0.85, (double)s, 0.15);
+            const double diff = t > r ? t - r : r - t;
+            if (diff > 0.001) {
+                p.rank[v] = (T)t;
+                p.c_new[v] = od ? (T)(t / (double)od) : (T)0;
+                nact++;
+            } else {
+                atomicAnd(&p.active[v >> 5], ~bit);
+                p.c_new[v] = p.c_old[v];
+            }
+        } else {
+            const double Vd = (double)V;
+            const T basev = (T)((1.0 - p.damping) / Vd + p.damping * (*p.dangling_prev) / Vd);
+            const T r = p.rank[v];
+            const T rn = basev + (T)p.damping * s;
+            res += fabs((double)rn - (double)r);
+            if (od == 0) dang += (double)rn;
+            p.rank[v] = rn;
+            p.c_new[v] = od ? rn / (T)od : (T)0;
+        }
+    }
+    if (REF) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) nact += __shfl_down_sync(kFull, nact, d);
+        if ((threadIdx.x & 31) == 0 && nact) atomicAdd(p.active_count, nact);
+    } else {
+        block_reduce2_atomic<T>(res, dang, p.acc, red);
+    }
+}
+
+template <typename T>
+__global__ void pr_push_init_kernel(T *rank, T *c0, T *c1, T *sum, const uint32_t *ptr, uint32_t *active, uint32_t V,
+                                    double *acc_pair) {
+    __shared__ double red[2 * kWarps];
+    double d = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < V; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        if (i < V) {
+            const double r = 1.0 / (double)V;
+            const uint32_t od = ptr[i + 1] - ptr[i];
+            rank[i] = (T)r;
+            const T c = od ? (T)(r / (double)od) : (T)0;
+            c0[i] = c;
+            c1[i] = c;
+            sum[i] = (T)0;
+            if (od == 0) d += (double)(T)r;
+        }
+        if (i < (V + 31) / 32) active[i] = 0xffffffffu;
+    }
+    block_reduce2_atomic<T>(0.0, d, acc_pair, red);
+}
+
+}  // namespace
+
+template <typename T, bool REF, int WORDS>
+static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *out, asc_stats *st) {
+    Workspace *ws = g->ws;
+    ASC_TRY(ensure_pr_buffers(g, sizeof(T)));
+    const uint32_t V = (uint32_t)g->V;
+    cudaStream_t s = g->stream;
+    uint32_t launches = 0;
+    double *acc = (double *)(ws->ctl + CTL_PR);   // residual/dangling pairs by pass parity
+    uint32_t *active_count = ws->ctl + CTL_PR + 8;  // word 40
+    T *rank = (T *)ws->pr_rank;
+    T *c[2] = {(T *)ws->pr_contrib[0], (T *)ws->pr_contrib[1]};
+    uint32_t *active = ws->bitmap[1];
+
+    ASC_CUDA(cudaEventRecord(ws->ev[0], s));
+    ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
+    pr_push_init_kernel<T><<<fill_grid(ws, V), kBlock, 0, s>>>(rank, c[0], c[1], (T *)ws->pr_sum, g->d_ptr, active, V,
+                                                               acc + 2);
+    launches++;
+    if (ws->n_huge_total) {
+        seed_huge_segments_kernel<<<fill_grid(ws, ws->n_huge_total), kBlock, 0, s>>>(
+            base_args(g, 1), ws->huge_list, ws->n_huge_static, ws->n_huge_total);
+        launches++;
+    }
+    ASC_CUDA(cudaGetLastError());
+    const int max_it = p.max_iterations > 0 ? p.max_iterations : (REF ? 1000000 : 100);
+    const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
+    int it = 0;
+    double residual = 0;
+    for (;;) {
+        if (it >= max_it) {
+            if (REF) return fail(ASC_ERR_TIMEOUT, "reference PageRank still active after %d passes", it);
+            break;
+        }
+        const int cp = it & 1;
+        ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK, 0, 4 * CTL_BLOCK, s));  // work cursors (block 1)
+        ASC_CUDA(cudaMemsetAsync(REF ? (void *)active_count : (void *)(acc + 2 * cp), 0, REF ? 4 : 16, s));
+        PushArgs<T> pa;
+        memset(&pa, 0, sizeof(pa));
+        pa.r0 = region_args(g, 0, 0, true);
+        pa.r1 = region_args(g, 0, 1, true);
+        pa.work = ws->ctl + CTL_BLOCK + 4;
+        pa.ptr = g->d_ptr;
+        pa.rank = rank;
+        pa.c_old = c[cp];
+        pa.c_new = c[1 - cp];
+        pa.sum = (T *)ws->pr_sum;
+        pa.active = active;
+        pa.active_count = active_count;
+        pa.damping = REF ? 0.85 : p.damping;
+        pa.acc = acc + 2 * cp;
+        pa.dangling_prev = acc + 2 * (1 - cp) + 1;
+        pr_scatter_kernel<T, WORDS><<<grid, kBlock, 0, s>>>(pa);
+        pr_push_apply_kernel<T, REF><<<fill_grid(ws, V), kBlock, 0, s>>>(pa, V);
+        launches += 2;
+        ASC_CUDA(cudaGetLastError());
+        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, REF ? (void *)active_count : (void *)(acc + 2 * cp), REF ? 4 : 16,
+                                 cudaMemcpyDeviceToHost, s));
+        ASC_CUDA(cudaStreamSynchronize(s));
+        it++;
+        if (REF) {
+            if (ws->h_ctl[0] == 0) break;
+        } else {
+            memcpy(&residual, ws->h_ctl, 8);
+            if (residual < p.tolerance) break;
+        }
+    }
+    ASC_CUDA(cudaEventRecord(ws->ev[1], s));
+    if (out && !(p.flags & ASC_RUN_NO_OUTPUT))
+        ASC_CUDA(cudaMemcpyAsync(out, rank, sizeof(T) * (size_t)V,
+                                 (p.flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 s));
+    ASC_CUDA(cudaEventRecord(ws->ev[2], s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 4, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        const unsigned long long *hs = (const unsigned long long *)(ws->h_ctl + CTL_STATS);
+        st->iterations = it;
+        st->edges_processed = hs[0] + hs[1];
+        st->ondemand_edges = hs[1];
+        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->frontier_vertices = hs[2] + hs[3];
+        st->ondemand_vertices = hs[3];
+        st->reached_vertices = V;
+        st->reached_edges = g->E;
+        st->residual = residual;
+        float ms = 0;
+        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[0], ws->ev[1]));
+        st->ms_total = ms;
+        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[1], ws->ev[2]));
+        st->ms_copyout = ms;
+        st->kernel_launches = launches;
+    }
+    return ASC_OK;
+}
+
 asc_status run_pagerank(asc_graph *g, const asc_params &p, void *out, asc_stats *st) {
     ASC_TRY(ensure_workspace(g));
+    if (!g->is_csc) {
+        const bool w2 = g->edge_words == 2;
+        if (p.pr_mode == ASC_PR_REF)
+            return w2 ? pagerank_push_impl<double, true, 2>(g, p, out, st)
+                      : pagerank_push_impl<double, true, 1>(g, p, out, st);
+        if (p.precision == ASC_F32)
+            return w2 ? pagerank_push_impl<float, false, 2>(g, p, out, st)
+                      : pagerank_push_impl<float, false, 1>(g, p, out, st);
+        return w2 ? pagerank_push_impl<double, false, 2>(g, p, out, st)
+                  : pagerank_push_impl<double, false, 1>(g, p, out, st);
+    }
     if (p.pr_mode == ASC_PR_REF) return pagerank_impl<double, true>(g, p, out, st);
     if (p.precision == ASC_F32) return pagerank_impl<float, false>(g, p, out, st);
     return pagerank_impl<double, false>(g, p, out, st);

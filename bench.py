@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--quick", action="store_true", help="BFS only (skip SSSP/CC legs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--split", action="store_true",
+                    help="profiling aid: time the steps with one launch per region (phase timing)")
+    ap.add_argument("--batch", type=int, default=64,
+                    help="sources of the multi-source leg (0 skips it)")
     return ap.parse_args()
 
 
@@ -192,8 +196,9 @@ def main():
     time.sleep(0.3)
     tot_edges, tot_ms, launches, od_bytes, iters = 0, 0.0, 0, 0, 0
     t_wall = time.perf_counter()
+    step_flags = A.RUN_NO_OUTPUT | (A.RUN_PHASE_TIMING if args.split else 0)
     for i in range(args.steps):
-        _, st = g.run("bfs", srcs[i % 8], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        _, st = g.run("bfs", srcs[i % 8], params=A.make_params(flags=step_flags))
         tot_edges += st["reached_edges"]
         tot_ms += st["ms_total"]
         launches += st["kernel_launches"]
@@ -263,6 +268,24 @@ def main():
                       "ondemand_bytes_per_bfs": int(od_bytes / args.steps), "iterations_per_bfs": iters / args.steps,
                       "generate_s": round(t_gen, 2)},
             "host_wall_ms_per_step": round(1e3 * t_wall / args.steps, 3)}
+    if args.batch:
+        # multi-source leg: one batch of up to 64 sources vs the same sources one at a time
+        bsrc = pick_sources(ptr, args.batch, args.seed + 100)
+        g.run_batch("bfs", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        _, bst = g.run_batch("bfs", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        seq_ms, seq_edges = 0.0, 0
+        for s_ in bsrc:
+            _, st = g.run("bfs", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+            seq_ms += st["ms_total"]
+            seq_edges += st["reached_edges"]
+        rows, _ = g.run_batch("bfs", bsrc[:4])
+        exact = all(np.array_equal(rows[i], g.run("bfs", s_)[0]) for i, s_ in enumerate(bsrc[:4]))
+        line["batch_bfs"] = {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
+                             "sequential_ms": round(seq_ms, 3),
+                             "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
+                             "batch_gteps": round(seq_edges / (bst["ms_total"] * 1e-3) / 1e9, 3),
+                             "ondemand_bytes": bst["ondemand_bytes"], "iterations": bst["iterations"],
+                             "rows_checked_bit_exact": 4, "bit_exact": bool(exact)}
     g.close()
 
     if not args.quick:
