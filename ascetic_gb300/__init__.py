@@ -39,7 +39,10 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_graph_open", "asc_graph_from_csr", "asc_graph_info_get", "asc_graph_close",
             "asc_params_default", "asc_run", "asc_bfs_opt", "asc_cc_opt", "asc_sssp_opt", "asc_pr_opt",
             "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe",
-            "asc_bfs_device_noalloc", "asc_run_batch"]
+            "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
+            "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
+            "asc_server_stats_get", "asc_server_destroy"]
+SERVE_BATCHED, SERVE_FIFO = 0, 1
 
 
 class EngineUnavailable(RuntimeError):
@@ -62,6 +65,27 @@ class GraphInfo(ctypes.Structure):
                 ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
                 ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_uint32),
+                ("queue_capacity", ctypes.c_uint32), ("mode", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class QueryInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("batch_size", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("cancelled", ctypes.c_uint64), ("batch_iterations", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_uint64), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double),
+                ("span_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Params(ctypes.Structure):
@@ -127,6 +151,14 @@ def lib():
         "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
         "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
         "asc_run_batch": ([c_vp, ctypes.c_int, c_vp, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
+        "asc_server_config_default": ([P(ServerConfig)], None),
+        "asc_server_create": ([P(ServerConfig), gpp], ctypes.c_int),
+        "asc_server_add_graph": ([c_vp, c_vp, P(c_u32)], ctypes.c_int),
+        "asc_server_submit": ([c_vp, c_u32, ctypes.c_int, c_u32, P(Params), c_vp, P(c_u64)], ctypes.c_int),
+        "asc_server_wait": ([c_vp, c_u64, ctypes.c_int64, P(QueryInfo)], ctypes.c_int),
+        "asc_server_cancel": ([c_vp, c_u64], ctypes.c_int),
+        "asc_server_stats_get": ([c_vp, P(ServerStats)], ctypes.c_int),
+        "asc_server_destroy": ([c_vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -280,6 +312,74 @@ def _run_batch(self, algo, sources, params=None, out=None, no_output=False):
 
 
 Graph.run_batch = _run_batch
+
+
+class Server:
+    """Query server over resident graphs (continuous batching or FIFO)."""
+
+    def __init__(self, budget_bytes=0, mode=SERVE_BATCHED, max_batch=64):
+        cfg = ServerConfig()
+        lib().asc_server_config_default(ctypes.byref(cfg))
+        cfg.device_budget_bytes, cfg.mode, cfg.max_batch = int(budget_bytes), mode, max_batch
+        h = ctypes.c_void_p()
+        _check(lib().asc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._graphs = []
+        self._out = {}
+
+    def add_graph(self, graph):
+        gid = ctypes.c_uint32()
+        _check(lib().asc_server_add_graph(self._h, graph._h, ctypes.byref(gid)))
+        self._graphs.append(graph)
+        return gid.value
+
+    def submit(self, graph_id, algo, source=0, params=None, out=None):
+        if isinstance(algo, str):
+            algo = ALGOS[algo]
+        p = params if params is not None else make_params()
+        if out is None:
+            g = self._graphs[graph_id]
+            dt = np.uint32 if algo != PR else (np.float32 if (p.pr_mode == PR_STD and p.precision == F32)
+                                                 else np.float64)
+            out = np.empty(g.V, dt)
+        t = ctypes.c_uint64()
+        _check(lib().asc_server_submit(self._h, graph_id, algo, source, ctypes.byref(p), out.ctypes.data,
+                                       ctypes.byref(t)))
+        self._out[t.value] = out
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        info = QueryInfo()
+        st = lib().asc_server_wait(self._h, ticket, timeout_ms, ctypes.byref(info))
+        out = self._out.pop(ticket, None)
+        if st not in (OK, ERR_CANCELLED):
+            raise AscError(st, last_error())
+        return out, {k: getattr(info, k) for k, _ in info._fields_ if k != "reserved"}
+
+    def cancel(self, ticket):
+        _check(lib().asc_server_cancel(self._h, ticket))
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().asc_server_stats_get(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().asc_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def rmat_csr(scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19, weights=None, symmetric=False,

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libascetic_gb300.so")
 PTGRAPH_PATH = os.path.join(LIB_DIR, "ptgraph")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["engine.cu", "graph.cpp", "capi.cpp"]
+LIB_SOURCES = ["engine.cu", "graph.cpp", "capi.cpp", "server.cpp"]
 
 
 def _nvcc():

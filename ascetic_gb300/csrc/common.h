@@ -44,6 +44,7 @@ struct Workspace {
     uint64_t V = 0;
     uint32_t *val = nullptr;         // u32 values (BFS/SSSP/CC)
     uint32_t *bitmap[2] = {nullptr, nullptr};  // frontier membership by parity, one bit per vertex
+    uint32_t *visited = nullptr;     // BFS: one bit per vertex already reached
     uint32_t *queue[2] = {nullptr, nullptr};   // [V]: static entries from 0, on-demand from S
     uint64_t *segs[2] = {nullptr, nullptr};    // segment items (v << 32 | k)
     uint64_t segcap_static = 0, segcap_ondemand = 0;
@@ -104,6 +105,19 @@ asc_status run_pagerank(asc_graph *g, const asc_params &p, void *out, asc_stats 
 asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params &p,
                      void *out, asc_stats *st);
 void free_workspace(asc_graph *g);
+// continuous multi-source batches (engine.cu)
+struct BatchEngine;
+uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride);
+uint64_t batch_plane_bytes(asc_graph *g);
+asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **out);
+void batch_destroy(BatchEngine *b);
+bool batch_has_plane(BatchEngine *b, uint32_t slot);
+asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source);
+bool batch_busy(const BatchEngine *b);
+asc_status batch_launch(BatchEngine *b);
+asc_status batch_collect(BatchEngine *b, uint64_t *finished);
+asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *host_out);
+uint64_t workspace_bytes(asc_graph *g, bool pagerank);
 // graph.cpp
 asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t param_size);
 }  // namespace asc

@@ -61,6 +61,7 @@ struct RegionArgs {
     const uint32_t *edges;        // region edge base, indexed by global edge offset
     uint32_t *val;
     uint32_t *bitmap;             // next-frontier bitmap (written)
+    uint32_t *visited;            // BFS: reached-vertex bitmap (claims)
     const uint32_t *bitmap_in;    // this iteration's frontier bitmap (null: no id-order mode)
     const uint32_t *q_in;         // this region's input list (null: dense range)
     const uint64_t *seg_in;       // this region's input segments
@@ -171,14 +172,33 @@ __device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint
     }
 }
 
+// What a thread reads about v before deciding to update it: BFS reads the
+// word of the reached-vertex bitmap (V/8 bytes, cache resident), the others
+// the value itself.
+template <int ALG>
+__device__ __forceinline__ uint32_t probe(const RegionArgs &a, uint32_t v) {
+    return ALG == kBFS ? a.visited[v >> 5] : a.val[v];
+}
+
 // Lowers val[v] to nv; true when this thread also won v's next-frontier bit.
-// cur is an earlier read of val[v]: values only decrease, so a stale read is
-// larger and can only cost an extra atomic, never a missed update.
+// cur is the earlier probe: reached bits and values only ever grow / shrink,
+// so a stale probe can only cost an extra atomic, never a missed update.
+// BFS is level-synchronous: every update of an iteration writes the same
+// level, so the first thread to set v's reached bit stores it and no atomicMin
+// is needed (the result equals the atomicMin relaxation's fixpoint).
+template <int ALG>
 __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t nv, uint32_t cur) {
+    const uint32_t bit = 1u << (v & 31);
+    if (ALG == kBFS) {
+        if (nv == 0xffffffffu || (cur & bit)) return false;
+        if (atomicOr(&a.visited[v >> 5], bit) & bit) return false;
+        a.val[v] = nv;
+        atomicOr(&a.bitmap[v >> 5], bit);
+        return true;
+    }
     if (nv >= cur) return false;
     uint32_t old = atomicMin(&a.val[v], nv);
     if (nv >= old) return false;
-    uint32_t bit = 1u << (v & 31);
     return (atomicOr(&a.bitmap[v >> 5], bit) & bit) == 0;
 }
 
@@ -236,9 +256,9 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
             }
         }
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? a.val[v[k]] : 0;
+        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_warp(a, lower(a, v[k], nv[k], cur[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) push_warp(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -265,9 +285,9 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item) {
             if (j < n) load_edge<ALG, WORDS>(a, vu, b + j, v[k], nv[k]);
         }
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? a.val[v[k]] : 0;
+        for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_warp(a, lower(a, v[k], nv[k], cur[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) push_warp(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
@@ -378,7 +398,10 @@ __global__ void seed_kernel(RegionArgs a, uint32_t src, uint32_t all) {
         const uint32_t i = base + threadIdx.x;
         const bool won = i < n;
         const uint32_t v = all ? i : src;
-        if (won) atomicOr(&a.bitmap[v >> 5], 1u << (v & 31));
+        if (won) {
+            atomicOr(&a.bitmap[v >> 5], 1u << (v & 31));
+            if (a.visited) atomicOr(&a.visited[v >> 5], 1u << (v & 31));
+        }
         push_warp(a, won, v);
     }
 }
@@ -670,10 +693,8 @@ __global__ void seed_huge_segments_kernel(RegionArgs a, const uint32_t *huge_lis
 
 // --------------------------------------------------------------- host -------
 
-asc_status ensure_workspace(asc_graph *g) {
-    if (g->ws) return ASC_OK;
-    Workspace *ws = new Workspace();
-    g->ws = ws;
+// Sizes and allocates the frontier machinery of one run for graph g.
+asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
     ws->V = g->V;
     ASC_CUDA(cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, g->device));
     {
@@ -708,6 +729,7 @@ asc_status ensure_workspace(asc_graph *g) {
     };
     ASC_TRY(dalloc((void **)&ws->val, 4 * V));
     for (int i = 0; i < 2; i++) ASC_TRY(dalloc((void **)&ws->bitmap[i], 4 * (V / 32 + 2)));
+    ASC_TRY(dalloc((void **)&ws->visited, 4 * (V / 32 + 2)));
     for (int i = 0; i < 2; i++) {
         ASC_TRY(dalloc((void **)&ws->queue[i], 4 * V));
         ASC_TRY(dalloc((void **)&ws->segs[i], 8 * (cs + co)));
@@ -720,6 +742,12 @@ asc_status ensure_workspace(asc_graph *g) {
     for (auto &e : ws->ev) ASC_CUDA(cudaEventCreate(&e));
     ws->device_bytes = bytes;
     return ASC_OK;
+}
+
+asc_status ensure_workspace(asc_graph *g) {
+    if (g->ws) return ASC_OK;
+    g->ws = new Workspace();
+    return alloc_workspace(g, g->ws);
 }
 
 asc_status ensure_pr_buffers(asc_graph *g, size_t elem) {
@@ -738,14 +766,14 @@ asc_status ensure_pr_buffers(asc_graph *g, size_t elem) {
     return ASC_OK;
 }
 
-RegionArgs base_args(asc_graph *g, int parity_in) {
-    Workspace *ws = g->ws;
+RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     RegionArgs a;
     memset(&a, 0, sizeof(a));
     a.ptr = g->d_ptr;
     a.val = ws->val;
     a.bitmap = ws->bitmap[1 - parity_in];
     a.bitmap_in = ws->bitmap[parity_in];
+    a.visited = ws->visited;
     a.dense_div = ws->tune.dense_div;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
@@ -761,9 +789,10 @@ RegionArgs base_args(asc_graph *g, int parity_in) {
     return a;
 }
 
-RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
-    Workspace *ws = g->ws;
-    RegionArgs a = base_args(g, parity_in);
+RegionArgs base_args(asc_graph *g, int parity_in) { return base_args(g, g->ws, parity_in); }
+
+RegionArgs region_args(asc_graph *g, Workspace *ws, int parity_in, int region, bool dense) {
+    RegionArgs a = base_args(g, ws, parity_in);
     a.region = region;
     a.edges = region == 0 ? g->d_static : g->d_host_edges;
     a.dense_begin = region == 0 ? 0 : g->static_vertices;
@@ -776,6 +805,10 @@ RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
     a.seg_in = ws->segs[parity_in] + (region == 0 ? 0 : ws->segcap_static);
     a.work = a.cnt_out + 4 + region;
     return a;
+}
+
+RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
+    return region_args(g, g->ws, parity_in, region, dense);
 }
 
 uint32_t grid_for(const Workspace *ws, uint64_t work_items) {
@@ -916,13 +949,12 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 
 }  // namespace
 
-void free_workspace(asc_graph *g) {
-    Workspace *ws = g->ws;
-    if (!ws) return;
+void free_ws_buffers(Workspace *ws) {
     for (void *p : {(void *)ws->ms_visit, (void *)ws->ms_front, (void *)ws->ms_next, (void *)ws->ms_touched,
                     (void *)ws->ms_out, (void *)ws->ms_dist})
         if (p) cudaFree(p);
-    for (void *p : {(void *)ws->val, (void *)ws->bitmap[0], (void *)ws->bitmap[1], (void *)ws->queue[0],
+    for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->bitmap[0], (void *)ws->bitmap[1],
+                    (void *)ws->queue[0],
                     (void *)ws->queue[1],
                     (void *)ws->segs[0], (void *)ws->segs[1], (void *)ws->ctl, (void *)ws->huge_list, ws->pr_rank,
                     ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
@@ -933,6 +965,12 @@ void free_workspace(asc_graph *g) {
     for (auto e : ws->ev)
         if (e) cudaEventDestroy(e);
     for (auto e : ws->phase_events) cudaEventDestroy(e);
+}
+
+void free_workspace(asc_graph *g) {
+    Workspace *ws = g->ws;
+    if (!ws) return;
+    free_ws_buffers(ws);
     delete ws;
     g->ws = nullptr;
 }
@@ -952,6 +990,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
     for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(ws->bitmap[i], 0, 4 * (V / 32 + 2), s));
+    ASC_CUDA(cudaMemsetAsync(ws->visited, 0, 4 * (V / 32 + 2), s));
     const uint32_t ig = fill_grid(ws, V);
     if (algo == ASC_CC) init_values_kernel<kCC><<<ig, kBlock, 0, s>>>(ws->val, V, 0);
     else if (algo == ASC_BFS) init_values_kernel<kBFS><<<ig, kBlock, 0, s>>>(ws->val, V, source);
@@ -1658,6 +1697,331 @@ asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint3
     return ASC_OK;
 }
 
+// ------------------------------------------- continuous multi-source batches --
+//
+// The serving loop keeps one batch per (graph, BFS | SSSP) whose 64 source
+// slots are filled and emptied between iterations: a query joins the running
+// batch as soon as a slot (and, for BFS, a level plane) is free, advances with
+// the other sources in shared iterations, and leaves when its own frontier is
+// empty. Levels are written relative to the iteration the source joined, so
+// every query's values equal a solo run from its source.
+struct BatchEngine {
+    asc_graph *g = nullptr;
+    bool sssp = false;
+    uint32_t stride = 64;             // SSSP distance row length (sources per row)
+    Workspace ws;                     // own frontier lists, bitmaps, counters
+    unsigned long long *visit = nullptr, *front = nullptr, *next = nullptr;
+    uint32_t *touched = nullptr;
+    uint32_t *dist = nullptr;         // SSSP [V][stride]
+    uint32_t *plane[64] = {nullptr};  // BFS per-slot level planes [V]
+    uint32_t **d_plane = nullptr;     // device copy of plane[]
+    int32_t *d_lvl_off = nullptr;     // per-slot level offset (level = iteration + offset)
+    int32_t lvl_off[64] = {0};
+    uint32_t *staging = nullptr;      // SSSP column gather [V]
+    cudaStream_t stream = nullptr;
+    int parity = 0;
+    uint32_t it = 0;                  // iterations run so far
+    uint64_t active = 0;              // slots in use
+    uint64_t joined_since_step = 0;   // slots admitted before the next iteration
+    uint32_t pend_n = 0, pend_slot[64], pend_src[64];
+    uint64_t bytes = 0;
+    uint32_t cnt[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+enum { CTL_ALIVE = 34 };  // u64 (words 34-35): OR of the new frontier masks of an iteration
+
+struct Admit {
+    uint32_t n;
+    uint32_t slot[64];
+    uint32_t src[64];
+};
+
+// Resets the per-slot state of newly admitted slots: BFS clears their bits in
+// every visited mask and fills their level planes, SSSP resets their distance
+// columns.
+__global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint32_t stride, uint32_t **planes,
+                                unsigned long long newmask, uint32_t V, uint32_t fill, uint32_t sssp) {
+    const uint64_t n = (uint64_t)V;
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        unsigned long long t = newmask;
+        if (!sssp) visit[v] &= ~newmask;
+        while (t) {
+            const int s = __ffsll((long long)t) - 1;
+            t &= t - 1;
+            if (sssp) dist[v * stride + s] = fill;
+            else planes[s][v] = fill;
+        }
+    }
+}
+
+// Admission, phase 1: a new source that is not in the current frontier gets a
+// fresh frontier mask (front[] of non-members may hold stale bits).
+__global__ void cb_admit_reset_kernel(Admit ad, unsigned long long *front, const uint32_t *bitmap_in) {
+    const uint32_t i = threadIdx.x;
+    if (i < ad.n) {
+        const uint32_t v = ad.src[i];
+        if (!((bitmap_in[v >> 5] >> (v & 31)) & 1u)) front[v] = 0;
+    }
+}
+
+// Admission, phase 2: mark each source at level / distance 1 and add it to the
+// current frontier (pushing the vertex when it was not a member yet).
+__global__ void cb_admit_kernel(Admit ad, MsArgs m, uint32_t **planes, uint32_t stride, uint32_t sssp) {
+    for (uint32_t base = 0; base < 64; base += 32) {
+        const uint32_t i = base + threadIdx.x;
+        bool won = false;
+        uint32_t v = 0;
+        if (i < ad.n) {
+            const uint32_t s = ad.slot[i];
+            v = ad.src[i];
+            const unsigned long long bit = 1ull << s;
+            if (sssp) m.dist[(uint64_t)v * stride + s] = 1;
+            else {
+                atomicOr(&m.visit[v], bit);
+                planes[s][v] = 1;
+            }
+            atomicOr(&m.front[v], bit);
+            won = !(atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31)) & (1u << (v & 31)));
+        }
+        push_warp(m.r0, won, v);
+    }
+}
+
+template <bool BFS>
+__global__ void cb_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_off, uint32_t it,
+                                unsigned long long *alive) {
+    const uint32_t n = *m.touched_cnt;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    unsigned long long any = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool won = false;
+        uint32_t v = 0;
+        if (i < n) {
+            v = m.touched[i];
+            unsigned long long nb = m.next[v];
+            m.next[v] = 0;
+            if (BFS) {
+                nb &= ~m.visit[v];
+                m.visit[v] |= nb;
+                unsigned long long t = nb;
+                while (t) {
+                    const int s = __ffsll((long long)t) - 1;
+                    t &= t - 1;
+                    planes[s][v] = (uint32_t)((int32_t)it + lvl_off[s]);
+                }
+            }
+            m.front[v] = nb;
+            any |= nb;
+            won = nb != 0;
+            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
+        }
+        push_warp(m.r0, won, v);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) any |= __shfl_down_sync(kFull, any, d);
+    if ((threadIdx.x & 31) == 0 && any) atomicOr(alive, any);
+}
+
+__global__ void cb_gather_column_kernel(const uint32_t *dist, uint32_t stride, uint32_t s, uint32_t *out, uint32_t V) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        out[v] = dist[(uint64_t)v * stride + s];
+}
+
+}  // namespace
+
+uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride) {
+    const uint64_t V = g->V;
+    uint64_t b = 28 * V + 16 * V + 3 * 4 * (V / 32 + 2) + 1024;  // masks, touched, lists, bitmaps
+    if (sssp) b += 4ull * V * stride + 4 * V;
+    return b;
+}
+
+uint64_t batch_plane_bytes(asc_graph *g) { return 4ull * g->V; }
+
+// Device bytes a graph's single-query state needs (estimate before the first
+// run; exact afterwards), with the PageRank buffers when asked for.
+uint64_t workspace_bytes(asc_graph *g, bool pagerank) {
+    const uint64_t V = g->V;
+    uint64_t b = g->ws ? g->ws->device_bytes : 4 * V + 3 * 4 * (V / 32 + 2) + 8 * V + 8 * (g->E / 256 + 1024) + 4096;
+    if (pagerank && (!g->ws || !g->ws->pr_rank)) b += 4ull * 8 * V;
+    return b;
+}
+
+void batch_destroy(BatchEngine *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    free_ws_buffers(&b->ws);
+    for (void *p : {(void *)b->visit, (void *)b->front, (void *)b->next, (void *)b->touched, (void *)b->dist,
+                    (void *)b->d_plane, (void *)b->d_lvl_off, (void *)b->staging})
+        if (p) cudaFree(p);
+    for (auto p : b->plane)
+        if (p) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **out) {
+    BatchEngine *b = new BatchEngine();
+    b->g = g;
+    b->sssp = sssp;
+    b->stride = stride;
+    asc_status st = alloc_workspace(g, &b->ws);
+    const uint64_t V = g->V;
+    auto al = [&](void **p, size_t n) {
+        if (st != ASC_OK) return;
+        cudaError_t e = cudaMalloc(p, n ? n : 16);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+    };
+    al((void **)&b->visit, 8 * V);
+    al((void **)&b->front, 8 * V);
+    al((void **)&b->next, 8 * V);
+    al((void **)&b->touched, 4 * V);
+    al((void **)&b->d_plane, 8 * 64);
+    al((void **)&b->d_lvl_off, 4 * 64);
+    if (sssp) {
+        al((void **)&b->dist, 4ull * V * stride);
+        al((void **)&b->staging, 4 * V);
+    }
+    if (st == ASC_OK) {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    // empty start state: no frontier, zero masks
+    if (st == ASC_OK) {
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->ws.ctl, 0, 4 * CTL_WORDS, b->stream);
+        for (int i = 0; i < 2 && e == cudaSuccess; i++)
+            e = cudaMemsetAsync(b->ws.bitmap[i], 0, 4 * (V / 32 + 2), b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->visit, 0, 8 * V, b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->front, 0, 8 * V, b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->next, 0, 8 * V, b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->d_plane, 0, 8 * 64, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "batch init", __FILE__, __LINE__);
+    }
+    if (st != ASC_OK) {
+        batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return ASC_OK;
+}
+
+bool batch_has_plane(BatchEngine *b, uint32_t slot) { return b->sssp || b->plane[slot] != nullptr; }
+
+// Queues a source for slot (joins before the next iteration). BFS slots need
+// their level plane; it is allocated here on first use.
+asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source) {
+    if (!b->sssp && !b->plane[slot]) {
+        ASC_CUDA(cudaMalloc(&b->plane[slot], 4ull * b->g->V));
+        ASC_CUDA(cudaMemcpyAsync(b->d_plane, b->plane, 8 * 64, cudaMemcpyHostToDevice, b->stream));
+    }
+    b->pend_slot[b->pend_n] = slot;
+    b->pend_src[b->pend_n] = source;
+    b->pend_n++;
+    b->active |= 1ull << slot;
+    b->joined_since_step |= 1ull << slot;
+    return ASC_OK;
+}
+
+bool batch_busy(const BatchEngine *b) { return b->active != 0; }
+
+// Applies the queued admissions and launches one iteration on the batch's
+// stream, ending with the readback of its counts (nothing waits here).
+asc_status batch_launch(BatchEngine *b) {
+    asc_graph *g = b->g;
+    Workspace *ws = &b->ws;
+    cudaStream_t s = b->stream;
+    const uint32_t V = (uint32_t)g->V;
+    const int p = b->parity, po = 1 - p;
+    MsArgs m;
+    memset(&m, 0, sizeof(m));
+    m.visit = b->visit;
+    m.front = b->front;
+    m.next = b->next;
+    m.touched = b->touched;
+    m.dist = b->dist;
+    m.V = V;
+    m.n = 64;
+    if (b->pend_n) {
+        Admit ad;
+        memset(&ad, 0, sizeof(ad));
+        ad.n = b->pend_n;
+        unsigned long long newmask = 0;
+        for (uint32_t i = 0; i < b->pend_n; i++) {
+            ad.slot[i] = b->pend_slot[i];
+            ad.src[i] = b->pend_src[i];
+            newmask |= 1ull << ad.slot[i];
+            b->lvl_off[ad.slot[i]] = 2 - (int32_t)(b->it + 1);  // found in the next iteration: level 2
+        }
+        ASC_CUDA(cudaMemcpyAsync(b->d_lvl_off, b->lvl_off, 4 * 64, cudaMemcpyHostToDevice, s));
+        cb_clear_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(b->visit, b->dist, b->stride, b->d_plane, newmask, V, V + 1,
+                                                             b->sssp ? 1 : 0);
+        RegionArgs in = base_args(g, ws, 1 - p);  // writes into the lists of parity p (this iteration's input)
+        cb_admit_reset_kernel<<<1, 64, 0, s>>>(ad, b->front, ws->bitmap[p]);
+        m.r0 = in;
+        cb_admit_kernel<<<1, 32, 0, s>>>(ad, m, b->d_plane, b->stride, b->sssp ? 1 : 0);
+        ASC_CUDA(cudaGetLastError());
+        b->pend_n = 0;
+    }
+    b->joined_since_step = 0;
+    uint32_t *touched_cnt = ws->ctl + CTL_PR;
+    unsigned long long *alive = (unsigned long long *)(ws->ctl + CTL_ALIVE);
+    ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
+    ASC_CUDA(cudaMemsetAsync(touched_cnt, 0, 4, s));
+    ASC_CUDA(cudaMemsetAsync(alive, 0, 8, s));
+    ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
+    m.r0 = region_args(g, ws, p, 0, false);
+    m.r1 = region_args(g, ws, p, 1, false);
+    m.work = m.r0.cnt_out + 4;
+    m.touched_cnt = touched_cnt;
+    const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
+    b->it++;
+    if (b->sssp) {
+        if (b->stride != 64) return fail(ASC_ERR_UNSUPPORTED, "SSSP batch rows of %u sources", b->stride);
+        m.r0.dense_div = m.r1.dense_div = 0;
+        ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
+        cb_apply_kernel<false><<<grid, kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it, alive);
+    } else {
+        if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
+        else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
+        cb_apply_kernel<true><<<grid, kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it, alive);
+    }
+    ASC_CUDA(cudaGetLastError());
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 16, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_ALIVE, alive, 8, cudaMemcpyDeviceToHost, s));
+    b->parity = po;
+    return ASC_OK;
+}
+
+// Waits for the launched iteration and reports the slots whose sources have
+// no frontier left (their values are final).
+asc_status batch_collect(BatchEngine *b, uint64_t *finished) {
+    ASC_CUDA(cudaStreamSynchronize(b->stream));
+    unsigned long long al = 0;
+    memcpy(&al, b->ws.h_ctl + CTL_ALIVE, 8);
+    *finished = b->active & ~al;
+    b->active &= al;
+    return ASC_OK;
+}
+
+// Copies a finished slot's values (V u32) to host memory.
+asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *host_out) {
+    const uint32_t V = (uint32_t)b->g->V;
+    if (b->sssp) {
+        cb_gather_column_kernel<<<fill_grid(&b->ws, V), kBlock, 0, b->stream>>>(b->dist, b->stride, slot, b->staging, V);
+        ASC_CUDA(cudaGetLastError());
+        ASC_CUDA(cudaMemcpyAsync(host_out, b->staging, 4ull * V, cudaMemcpyDeviceToHost, b->stream));
+    } else {
+        ASC_CUDA(cudaMemcpyAsync(host_out, b->plane[slot], 4ull * V, cudaMemcpyDeviceToHost, b->stream));
+    }
+    ASC_CUDA(cudaStreamSynchronize(b->stream));
+    return ASC_OK;
+}
+
 // ------------------------------------------------- PageRank over CSR graphs --
 //
 // Graphs stored by out-edges (.bcsr / .bwcsr) run PageRank by scatter: every
@@ -2089,11 +2453,12 @@ constexpr uint64_t kNoAllocMaxSegs = kNoAllocMaxE / kNoAllocSeg + kNoAllocMaxE /
 constexpr uint64_t na_round(uint64_t x) { return (x + 255) & ~255ull; }
 constexpr uint64_t kNaCtl = 0;
 constexpr uint64_t kNaBitmap = na_round(kNaCtl + 4 * CTL_WORDS);
-constexpr uint64_t kNaQueue0 = na_round(kNaBitmap + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaVisited = na_round(kNaBitmap + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaQueue0 = na_round(kNaVisited + 4 * (kNoAllocMaxV / 32 + 2));
 constexpr uint64_t kNaQueue1 = na_round(kNaQueue0 + 4 * kNoAllocMaxV);
 constexpr uint64_t kNaSegs0 = na_round(kNaQueue1 + 4 * kNoAllocMaxV);
 constexpr uint64_t kNaSegs1 = na_round(kNaSegs0 + 8 * kNoAllocMaxSegs);
-constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // about 9.2 MB
+constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // about 9.3 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -2152,6 +2517,7 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     cudaStream_t s = (cudaStream_t)stream;
     uint32_t *ctl = (uint32_t *)(base + kNaCtl);
     uint32_t *bitmap = (uint32_t *)(base + kNaBitmap);
+    uint32_t *visited = (uint32_t *)(base + kNaVisited);
     uint32_t *queue[2] = {(uint32_t *)(base + kNaQueue0), (uint32_t *)(base + kNaQueue1)};
     uint64_t *segs[2] = {(uint64_t *)(base + kNaSegs0), (uint64_t *)(base + kNaSegs1)};
     const uint32_t V32 = (uint32_t)V, E32 = (uint32_t)E;
@@ -2160,8 +2526,10 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     ASC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const uint32_t fill = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((V + kBlock - 1) / kBlock, sms * 8ull));
 
-    // the array keeps the previous call's contents: clear the counters first
+    // the array keeps the previous call's contents: clear the counters and the
+    // reached-vertex bitmap first
     ASC_CUDA(cudaMemsetAsync(ctl, 0, 4 * CTL_WORDS, s));
+    ASC_CUDA(cudaMemsetAsync(visited, 0, 4 * (V / 32 + 2), s));
     noalloc_validate_kernel<<<fill, kBlock, 0, s>>>(d_row_offsets, d_col, V32, E32, ctl + CTL_PR);
     ASC_CUDA(cudaGetLastError());
     uint32_t flag = 0;
@@ -2178,6 +2546,7 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     a.edges = d_col;
     a.val = d_levels;
     a.bitmap = bitmap;
+    a.visited = visited;
     a.S = V32;  // the whole graph is device resident: one region
     a.V = V32;
     a.huge = kNoAllocHuge;

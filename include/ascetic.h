@@ -191,6 +191,65 @@ asc_status asc_sssp_opt(const char *path, uint32_t source, double advise_rate, u
                         asc_stats *stats);
 asc_status asc_pr_opt(const char *path, double advise_rate, double *out, asc_stats *stats);
 
+/* ---- query server ----------------------------------------------------------- */
+/* Serves BFS / SSSP / CC / PageRank queries against several resident graphs on
+ * one GPU under one device-memory budget. In ASC_SERVE_BATCHED mode BFS and
+ * SSSP queries are batched continuously: a query joins the running
+ * multi-source batch of its graph as soon as a source slot and memory are
+ * free, shares every later iteration with the other sources (one edge read
+ * serves all of them), and completes when its own frontier is empty; its
+ * values are identical to a solo asc_run. CC and PageRank queries run whole;
+ * identical pending ones share one run. ASC_SERVE_FIFO is the plain engine:
+ * one query at a time, in arrival order. The server is internally
+ * synchronised; graphs stay owned by the caller and must outlive the server.
+ * No reference counterpart (the reference answers one query per process). */
+typedef struct asc_server asc_server;
+enum { ASC_SERVE_BATCHED = 0, ASC_SERVE_FIFO = 1 };
+
+typedef struct asc_server_config {
+    uint64_t device_budget_bytes; /* every device allocation of the graphs and queries (0 = no cap) */
+    uint32_t max_batch;           /* sources per batch, 1..64 (0 = 64) */
+    uint32_t queue_capacity;      /* queries in flight before ASC_ERR_BUSY (0 = 2^20) */
+    uint32_t mode;                /* ASC_SERVE_BATCHED or ASC_SERVE_FIFO */
+    uint32_t reserved;
+} asc_server_config;
+
+typedef struct asc_query_info {
+    int32_t status;       /* asc_status of the query */
+    int32_t iterations;   /* iterations of the run that answered it (whole runs) */
+    uint32_t batch_size;  /* sources sharing its batch when it finished, or queries sharing its run */
+    uint32_t reserved;
+    double queue_ms;      /* submit to start */
+    double latency_ms;    /* submit to completion */
+} asc_query_info;
+
+typedef struct asc_server_stats {
+    uint64_t submitted, completed, failed, cancelled;
+    uint64_t batch_iterations;
+    uint64_t device_bytes;  /* device bytes accounted against the budget */
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* completed-query latency */
+    double queries_per_s;   /* completed / (last completion - first submit) */
+    double span_s;
+} asc_server_stats;
+
+void asc_server_config_default(asc_server_config *c);
+asc_status asc_server_create(const asc_server_config *cfg, asc_server **out);
+/* Registers a graph (before the first query); its static region and offsets
+ * count against the budget. */
+asc_status asc_server_add_graph(asc_server *s, asc_graph *g, uint32_t *graph_id);
+/* Queues a query; out (host memory, V values like asc_run, may be NULL) is
+ * written before the query completes. */
+asc_status asc_server_submit(asc_server *s, uint32_t graph_id, asc_algo algo, uint32_t source,
+                             const asc_params *params, void *out, uint64_t *ticket);
+/* Waits for a query (timeout_ms < 0: no limit) and releases its ticket;
+ * returns the query's status. */
+asc_status asc_server_wait(asc_server *s, uint64_t ticket, int64_t timeout_ms, asc_query_info *info);
+/* Cancels a query that has not started (it completes with ASC_ERR_CANCELLED). */
+asc_status asc_server_cancel(asc_server *s, uint64_t ticket);
+asc_status asc_server_stats_get(asc_server *s, asc_server_stats *out);
+/* Finishes running work, cancels queued queries and frees the server's state. */
+asc_status asc_server_destroy(asc_server *s);
+
 /* ---- synthetic graphs and files -------------------------------------------- */
 enum {
     ASC_RMAT_WEIGHTS = 1u << 0,    /* emit {dst, weight} pairs, weight uniform in [wmin, wmax] */
@@ -229,7 +288,7 @@ asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double
  * the BFS has finished on it.
  * Limits: V <= 1,048,576 and E <= 16,777,216; larger graphs return
  * ASC_ERR_BUDGET. The CSR is checked on the device first (ASC_ERR_INVALID).
- * Scratch: one fixed device array of about 9.2 MB in this library, held by
+ * Scratch: one fixed device array of about 9.3 MB in this library, held by
  * every GPU that loads it until the process exits; no cudaMalloc, cudaFree or
  * allocating library routine is called. The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current, so
