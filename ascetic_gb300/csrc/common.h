@@ -45,6 +45,7 @@ struct Workspace {
     uint32_t *val = nullptr;         // u32 values (BFS/SSSP/CC)
     uint32_t *bitmap[2] = {nullptr, nullptr};  // frontier membership by parity, one bit per vertex
     uint32_t *visited = nullptr;     // BFS: one bit per vertex already reached
+    uint32_t *huge_bits = nullptr;   // one bit per vertex with more than huge_degree edges
     uint32_t *queue[2] = {nullptr, nullptr};   // [V]: static entries from 0, on-demand from S
     uint64_t *segs[2] = {nullptr, nullptr};    // segment items (v << 32 | k)
     uint64_t segcap_static = 0, segcap_ondemand = 0;

@@ -47,7 +47,8 @@ enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 
 // Control block (u32 words). Per parity p: [8p+0..3] counts of the frontier
 // built for that parity (static list, on-demand list, static segments,
-// on-demand segments), [8p+4..5] work cursors of the launches that build it.
+// on-demand segments), [8p+4..5] work cursors of the launches that build it,
+// [8p+6..7] vertices of each region in that frontier (its bitmap's bits).
 // Stats at word 16 (u64): edges static, edges on-demand, frontier vertices
 // static, frontier vertices on-demand, reached vertices, reached edges. PageRank FP64 accumulators at word 32:
 // residual[2], dangling[2].
@@ -62,6 +63,7 @@ struct RegionArgs {
     uint32_t *val;
     uint32_t *bitmap;             // next-frontier bitmap (written)
     uint32_t *visited;            // BFS: reached-vertex bitmap (claims)
+    const uint32_t *huge_bits;    // one bit per vertex whose list is cut into segments
     const uint32_t *bitmap_in;    // this iteration's frontier bitmap (null: no id-order mode)
     const uint32_t *q_in;         // this region's input list (null: dense range)
     const uint64_t *seg_in;       // this region's input segments
@@ -175,6 +177,17 @@ __device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint
 // What a thread reads about v before deciding to update it: BFS reads the
 // word of the reached-vertex bitmap (V/8 bytes, cache resident), the others
 // the value itself.
+// Counts, per region, the vertices whose next-frontier bit this warp won
+// (shared-memory counters, flushed once per CTA). Every lane calls it.
+__device__ __forceinline__ void count_next(const RegionArgs &a, bool won, uint32_t v, uint32_t *s_next) {
+    const unsigned m0 = __ballot_sync(kFull, won && v < a.S);
+    const unsigned m1 = __ballot_sync(kFull, won && v >= a.S);
+    if ((threadIdx.x & 31) == 0) {
+        if (m0) atomicAdd(&s_next[0], (uint32_t)__popc(m0));
+        if (m1) atomicAdd(&s_next[1], (uint32_t)__popc(m1));
+    }
+}
+
 template <int ALG>
 __device__ __forceinline__ uint32_t probe(const RegionArgs &a, uint32_t v) {
     return ALG == kBFS ? a.visited[v >> 5] : a.val[v];
@@ -208,7 +221,8 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
 constexpr int kUnroll = 4;
 
 template <int ALG, int WORDS>
-__device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, Smem &sm) {
+__device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, Smem &sm,
+                            uint32_t *s_next) {
     const uint32_t i = tile * kBlock + threadIdx.x;
     bool act;
     uint32_t u;
@@ -258,7 +272,7 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_warp(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -268,7 +282,7 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
 }
 
 template <int ALG, int WORDS>
-__device__ void expand_segment(const RegionArgs &a, uint64_t item) {
+__device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_next) {
     const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
     const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
     const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
@@ -287,7 +301,7 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_warp(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
@@ -307,21 +321,51 @@ __device__ __forceinline__ void region_items(const RegionArgs &a, uint32_t &n_in
     items = nseg + (nvert + kBlock - 1) / kBlock;
 }
 
+// Work of one region for the bitmap-built frontier: a region whose frontier
+// holds more than 1/dense_div of its vertices is walked through the bitmap in
+// id order (its list was not built), otherwise through its list.
+__device__ __forceinline__ void region_items_bits(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg,
+                                                  uint32_t &items, int &mode) {
+    const uint32_t range = a.dense_end - a.dense_begin;
+    const uint32_t bits = a.cnt_in[6 + a.region];
+    nseg = a.cnt_in[2 + a.region];
+    if (a.bitmap_in && a.dense_div && bits > range / a.dense_div) {
+        mode = kBitmap;
+        n_in = 0;
+    } else {
+        mode = kList;
+        n_in = a.cnt_in[a.region];
+    }
+    const uint32_t nvert = mode == kList ? n_in : range;
+    items = nseg + (nvert + kBlock - 1) / kBlock;
+}
+
+__device__ __forceinline__ void flush_next(const RegionArgs &a, uint32_t *s_next) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_next[0]) atomicAdd(&a.cnt_out[6], s_next[0]);
+        if (s_next[1]) atomicAdd(&a.cnt_out[7], s_next[1]);
+    }
+}
+
 template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
     __shared__ Smem sm;
+    __shared__ uint32_t s_next[2];
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     uint32_t n_in, nseg, total;
     int mode;
-    region_items(a, n_in, nseg, total, mode);
+    region_items_bits(a, n_in, nseg, total, mode);
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(a.work, 1u);
         __syncthreads();
         const uint32_t w = sm.work;
         __syncthreads();
         if (w >= total) break;
-        if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w]);
-        else expand_tile<ALG, WORDS>(a, w - nseg, n_in, mode, sm);
+        if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w], s_next);
+        else expand_tile<ALG, WORDS>(a, w - nseg, n_in, mode, sm, s_next);
     }
+    flush_next(a, s_next);
 }
 
 // Both regions in one launch. Work items alternate between the on-demand and
@@ -336,10 +380,12 @@ struct FusedArgs {
 template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
     __shared__ Smem sm;
+    __shared__ uint32_t s_next[2];
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     uint32_t n0, s0, i0, n1, s1, i1;
     int m0, m1;
-    region_items(x.r0, n0, s0, i0, m0);
-    region_items(x.r1, n1, s1, i1, m1);
+    region_items_bits(x.r0, n0, s0, i0, m0);
+    region_items_bits(x.r1, n1, s1, i1, m1);
     const uint32_t m = min(i0, i1), total = i0 + i1;
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(x.work, 1u);
@@ -357,12 +403,115 @@ __global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
             local = m + (w - 2 * m);
         }
         if (od) {
-            if (local < s1) expand_segment<ALG, WORDS>(x.r1, x.r1.seg_in[local]);
-            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, m1, sm);
+            if (local < s1) expand_segment<ALG, WORDS>(x.r1, x.r1.seg_in[local], s_next);
+            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, m1, sm, s_next);
         } else {
-            if (local < s0) expand_segment<ALG, WORDS>(x.r0, x.r0.seg_in[local]);
-            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, m0, sm);
+            if (local < s0) expand_segment<ALG, WORDS>(x.r0, x.r0.seg_in[local], s_next);
+            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, m0, sm, s_next);
         }
+    }
+    flush_next(x.r0, s_next);
+}
+
+// Builds the next frontier from its bitmap (one thread per 32-vertex word):
+// vertices with long lists become segment items; the others are appended to
+// their region's list only when that region will be walked as a list (warp
+// scan of the per-word counts, one atomic per warp). cnt_out[6..7] hold the
+// region bit counts the expansion flushed; cnt_out[0..3] receive the lists.
+__global__ void build_frontier_kernel(RegionArgs a, const uint32_t *next_bits, uint32_t nwords) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t range0 = a.S, range1 = a.V - a.S;
+    const bool list0 = !(a.dense_div && a.cnt_out[6] > range0 / a.dense_div);
+    const bool list1 = !(a.dense_div && a.cnt_out[7] > range1 / a.dense_div);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nwords; base += stride) {
+        const uint32_t w = base + threadIdx.x;
+        uint32_t word = 0, hw = 0;
+        if (w < nwords) {
+            word = next_bits[w];
+            hw = word & a.huge_bits[w];
+        }
+        // long lists: one thread per vertex appends its segments (rare)
+        while (hw) {
+            const int b = __ffs(hw) - 1;
+            hw &= hw - 1;
+            const uint32_t v = 32 * w + b;
+            const uint32_t deg = a.ptr[v + 1] - a.ptr[v];
+            const uint32_t nseg = (deg + a.seg_len - 1) / a.seg_len;
+            const bool od = v >= a.S;
+            const uint32_t sb = atomicAdd(&a.cnt_out[2 + od], nseg);
+            uint64_t *dst = a.seg_out + (od ? a.segcap_static : 0) + sb;
+            for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
+        }
+        if (w < nwords) word &= ~a.huge_bits[w];
+        // region split of this word: bits of vertices below S are static
+        uint32_t smask;
+        const uint32_t v0 = 32 * w;
+        if (v0 + 32 <= a.S) smask = 0xffffffffu;
+        else if (v0 >= a.S) smask = 0;
+        else smask = (1u << (a.S - v0)) - 1u;
+        const uint32_t w0 = list0 ? (word & smask) : 0, w1 = list1 ? (word & ~smask) : 0;
+        const uint32_t c0 = __popc(w0), c1 = __popc(w1);
+        uint32_t i0 = c0, i1 = c1;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y0 = __shfl_up_sync(kFull, i0, d), y1 = __shfl_up_sync(kFull, i1, d);
+            if (lane >= d) {
+                i0 += y0;
+                i1 += y1;
+            }
+        }
+        const uint32_t t0 = __shfl_sync(kFull, i0, 31), t1 = __shfl_sync(kFull, i1, 31);
+        uint32_t b0 = 0, b1 = 0;
+        if (lane == 0) {
+            if (t0) b0 = atomicAdd(&a.cnt_out[0], t0);
+            if (t1) b1 = atomicAdd(&a.cnt_out[1], t1);
+        }
+        b0 = __shfl_sync(kFull, b0, 0) + i0 - c0;
+        b1 = __shfl_sync(kFull, b1, 0) + i1 - c1;
+        uint32_t x = w0;
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            a.q_out[b0++] = v0 + b;
+        }
+        x = w1;
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            a.q_out[a.S + b1++] = v0 + b;
+        }
+    }
+}
+
+// First frontier of a traversal: one source, or every vertex (CC); sets its
+// bits and region counts in the parity-0 block.
+__global__ void seed_bits_kernel(RegionArgs a, uint32_t src, uint32_t all, uint32_t nwords) {
+    if (!all) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.bitmap[src >> 5] |= 1u << (src & 31);
+            if (a.visited) a.visited[src >> 5] |= 1u << (src & 31);
+            a.cnt_out[src < a.S ? 6 : 7] = 1;
+        }
+        return;
+    }
+    uint32_t n0 = 0, n1 = 0;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const uint32_t v0 = 32 * w;
+        uint32_t m = v0 + 32 <= a.V ? 0xffffffffu : (v0 < a.V ? (1u << (a.V - v0)) - 1u : 0);
+        a.bitmap[w] = m;
+        uint32_t smask = v0 + 32 <= a.S ? 0xffffffffu : (v0 >= a.S ? 0 : (1u << (a.S - v0)) - 1u);
+        n0 += __popc(m & smask);
+        n1 += __popc(m & ~smask);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        n0 += __shfl_down_sync(kFull, n0, d);
+        n1 += __shfl_down_sync(kFull, n1, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (n0) atomicAdd(&a.cnt_out[6], n0);
+        if (n1) atomicAdd(&a.cnt_out[7], n1);
     }
 }
 
@@ -372,8 +521,8 @@ __global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
 // non-empty, counts the iterations that had input, and stops at the cap.
 __global__ void loop_cond_kernel(cudaGraphConditionalHandle h, uint32_t *ctl, uint32_t cap) {
     const uint32_t *b0 = ctl, *b1 = ctl + CTL_BLOCK;
-    const bool second = (b1[0] | b1[1] | b1[2] | b1[3]) != 0;
-    bool more = (b0[0] | b0[1] | b0[2] | b0[3]) != 0;
+    const bool second = (b1[6] | b1[7]) != 0;
+    bool more = (b0[6] | b0[7]) != 0;
     const uint32_t it = ctl[CTL_ITERS] + 1 + (second ? 1 : 0);
     ctl[CTL_ITERS] = it;
     ctl[CTL_BODIES] += 1;
@@ -718,6 +867,8 @@ asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
         }
     }
     ws->n_huge_total = (uint32_t)huge.size();
+    std::vector<uint32_t> hbits(V / 32 + 2, 0);
+    for (uint32_t v : huge) hbits[v >> 5] |= 1u << (v & 31);
     ws->segcap_static = cs;
     ws->segcap_ondemand = co;
     uint64_t bytes = 0;
@@ -730,6 +881,8 @@ asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
     ASC_TRY(dalloc((void **)&ws->val, 4 * V));
     for (int i = 0; i < 2; i++) ASC_TRY(dalloc((void **)&ws->bitmap[i], 4 * (V / 32 + 2)));
     ASC_TRY(dalloc((void **)&ws->visited, 4 * (V / 32 + 2)));
+    ASC_TRY(dalloc((void **)&ws->huge_bits, 4 * (V / 32 + 2)));
+    ASC_CUDA(cudaMemcpy(ws->huge_bits, hbits.data(), 4 * (V / 32 + 2), cudaMemcpyHostToDevice));
     for (int i = 0; i < 2; i++) {
         ASC_TRY(dalloc((void **)&ws->queue[i], 4 * V));
         ASC_TRY(dalloc((void **)&ws->segs[i], 8 * (cs + co)));
@@ -774,6 +927,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.bitmap = ws->bitmap[1 - parity_in];
     a.bitmap_in = ws->bitmap[parity_in];
     a.visited = ws->visited;
+    a.huge_bits = ws->huge_bits;
     a.dense_div = ws->tune.dense_div;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
@@ -927,6 +1081,8 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
                     x.r1 = region_args(g, parity, 1, false);
                     x.work = x.r0.cnt_out + 4;
                     fused(cs, x, grid);
+                    build_frontier_kernel<<<fill_grid(ws, V / 32 + 1), kBlock, 0, cs>>>(x.r0, ws->bitmap[po],
+                                                                                        V / 32 + 1);
                 }
                 loop_cond_kernel<<<1, 1, 0, cs>>>(handle, ws->ctl, cap);
                 cudaGraph_t out = nullptr;
@@ -953,7 +1109,8 @@ void free_ws_buffers(Workspace *ws) {
     for (void *p : {(void *)ws->ms_visit, (void *)ws->ms_front, (void *)ws->ms_next, (void *)ws->ms_touched,
                     (void *)ws->ms_out, (void *)ws->ms_dist})
         if (p) cudaFree(p);
-    for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->bitmap[0], (void *)ws->bitmap[1],
+    for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->bitmap[0],
+                    (void *)ws->bitmap[1],
                     (void *)ws->queue[0],
                     (void *)ws->queue[1],
                     (void *)ws->segs[0], (void *)ws->segs[1], (void *)ws->ctl, (void *)ws->huge_list, ws->pr_rank,
@@ -997,8 +1154,10 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     else init_values_kernel<kSSSP><<<ig, kBlock, 0, s>>>(ws->val, V, source);
     // the seeded frontier lands in parity 0 (as the output of a virtual pass from parity 1)
     RegionArgs sa = base_args(g, 1);
-    seed_kernel<<<all ? fill_grid(ws, V) : 1, kBlock, 0, s>>>(sa, source, all ? 1 : 0);
-    launches += 2;
+    const uint32_t nwords = V / 32 + 1;
+    seed_bits_kernel<<<all ? fill_grid(ws, nwords) : 1, kBlock, 0, s>>>(sa, source, all ? 1 : 0, nwords);
+    build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(sa, ws->bitmap[0], nwords);
+    launches += 3;
     ASC_CUDA(cudaGetLastError());
     const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
     const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP));
@@ -1011,14 +1170,20 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         ASC_CUDA(cudaGraphLaunch(ws->loop_exec[slot], s));
         launches += 1;
     }
-    uint32_t cnt[4] = {0, 0, 0, 0};
+    uint32_t cnt[CTL_BLOCK] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (!use_graph) {
         ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
         ASC_CUDA(cudaStreamSynchronize(s));
         memcpy(cnt, ws->h_ctl, sizeof(cnt));
     }
     int parity = 0;
-    while (cnt[0] | cnt[1] | cnt[2] | cnt[3]) {
+    const uint32_t div = ws->tune.dense_div;
+    auto region_work = [&](int region) -> uint64_t {
+        const uint32_t range = region == 0 ? g->static_vertices : V - g->static_vertices;
+        const bool bitmap_mode = div && cnt[6 + region] > range / div;
+        return (uint64_t)cnt[2 + region] + ((bitmap_mode ? range : cnt[region]) + kBlock - 1) / kBlock;
+    };
+    while (cnt[6] | cnt[7]) {
         if (iters >= cap) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
         iters++;
         const int po = 1 - parity;
@@ -1027,7 +1192,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         if (pt.on) {
             // diagnostic: one launch per region, each timed on its own
             for (int region = 0; region < 2; region++) {
-                const uint64_t items = (uint64_t)cnt[2 + region] + (cnt[region] + kBlock - 1) / kBlock;
+                const uint64_t items = region_work(region);
                 if (!items) continue;
                 RegionArgs a = region_args(g, parity, region, false);
                 ASC_TRY(pt.begin(region));
@@ -1037,8 +1202,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
                 launches++;
             }
         } else {
-            const uint64_t items = (uint64_t)cnt[2] + (cnt[0] + kBlock - 1) / kBlock + (uint64_t)cnt[3] +
-                                   (cnt[1] + kBlock - 1) / kBlock;
+            const uint64_t items = region_work(0) + region_work(1);
             FusedArgs x;
             x.r0 = region_args(g, parity, 0, false);
             x.r1 = region_args(g, parity, 1, false);
@@ -1046,8 +1210,11 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
             fused(s, x, grid_for(ws, items));
             launches++;
         }
+        build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(region_args(g, parity, 0, false),
+                                                                        ws->bitmap[po], nwords);
+        launches++;
         ASC_CUDA(cudaGetLastError());
-        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 4 * 4, cudaMemcpyDeviceToHost, s));
+        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
         ASC_CUDA(cudaStreamSynchronize(s));
         memcpy(cnt, ws->h_ctl, sizeof(cnt));
         if (pt.on) ASC_TRY(pt.sum(phase_ms));
@@ -1071,7 +1238,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     ASC_CUDA(cudaStreamSynchronize(s));
     if (use_graph) {
         iters = (int)ws->h_ctl[CTL_ITERS];
-        launches += 3 * ws->h_ctl[CTL_BODIES] - 1;  // two expansions and the loop test per body
+        launches += 5 * ws->h_ctl[CTL_BODIES] - 1;  // two expansions, two builds and the loop test per body
         if (ws->h_ctl[CTL_TIMEOUT]) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
     }
     if (st) {
@@ -2453,12 +2620,14 @@ constexpr uint64_t kNoAllocMaxSegs = kNoAllocMaxE / kNoAllocSeg + kNoAllocMaxE /
 constexpr uint64_t na_round(uint64_t x) { return (x + 255) & ~255ull; }
 constexpr uint64_t kNaCtl = 0;
 constexpr uint64_t kNaBitmap = na_round(kNaCtl + 4 * CTL_WORDS);
-constexpr uint64_t kNaVisited = na_round(kNaBitmap + 4 * (kNoAllocMaxV / 32 + 2));
-constexpr uint64_t kNaQueue0 = na_round(kNaVisited + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaBitmap1 = na_round(kNaBitmap + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaVisited = na_round(kNaBitmap1 + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaHuge = na_round(kNaVisited + 4 * (kNoAllocMaxV / 32 + 2));
+constexpr uint64_t kNaQueue0 = na_round(kNaHuge + 4 * (kNoAllocMaxV / 32 + 2));
 constexpr uint64_t kNaQueue1 = na_round(kNaQueue0 + 4 * kNoAllocMaxV);
 constexpr uint64_t kNaSegs0 = na_round(kNaQueue1 + 4 * kNoAllocMaxV);
 constexpr uint64_t kNaSegs1 = na_round(kNaSegs0 + 8 * kNoAllocMaxSegs);
-constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // about 9.3 MB
+constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // about 9.6 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -2479,6 +2648,19 @@ __global__ void noalloc_validate_kernel(const uint32_t *ptr, const uint32_t *col
         if (ptr[v] > ptr[v + 1]) atomicOr(flag, 2u);
     for (uint32_t i = t; i < E; i += stride)
         if (col[i] >= V) atomicOr(flag, 4u);
+}
+
+// One bit per vertex whose list is longer than the huge-degree threshold.
+__global__ void noalloc_huge_bits_kernel(const uint32_t *ptr, uint32_t V, uint32_t huge, uint32_t *bits,
+                                         uint32_t nwords) {
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        uint32_t m = 0;
+        for (uint32_t b = 0; b < 32; b++) {
+            const uint32_t v = 32 * w + b;
+            if (v < V && ptr[v + 1] - ptr[v] > huge) m |= 1u << b;
+        }
+        bits[w] = m;
+    }
 }
 
 asc_status noalloc_scratch(unsigned char **out) {
@@ -2516,20 +2698,23 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     ASC_TRY(noalloc_scratch(&base));
     cudaStream_t s = (cudaStream_t)stream;
     uint32_t *ctl = (uint32_t *)(base + kNaCtl);
-    uint32_t *bitmap = (uint32_t *)(base + kNaBitmap);
+    uint32_t *bitmap[2] = {(uint32_t *)(base + kNaBitmap), (uint32_t *)(base + kNaBitmap1)};
     uint32_t *visited = (uint32_t *)(base + kNaVisited);
+    uint32_t *huge_bits = (uint32_t *)(base + kNaHuge);
     uint32_t *queue[2] = {(uint32_t *)(base + kNaQueue0), (uint32_t *)(base + kNaQueue1)};
     uint64_t *segs[2] = {(uint64_t *)(base + kNaSegs0), (uint64_t *)(base + kNaSegs1)};
     const uint32_t V32 = (uint32_t)V, E32 = (uint32_t)E;
+    const uint32_t nwords = V32 / 32 + 1;
     int dev = 0, sms = 0;
     ASC_CUDA(cudaGetDevice(&dev));
     ASC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const uint32_t fill = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((V + kBlock - 1) / kBlock, sms * 8ull));
 
     // the array keeps the previous call's contents: clear the counters and the
-    // reached-vertex bitmap first
+    // bitmaps first
     ASC_CUDA(cudaMemsetAsync(ctl, 0, 4 * CTL_WORDS, s));
     ASC_CUDA(cudaMemsetAsync(visited, 0, 4 * (V / 32 + 2), s));
+    for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(bitmap[i], 0, 4 * (V / 32 + 2), s));
     noalloc_validate_kernel<<<fill, kBlock, 0, s>>>(d_row_offsets, d_col, V32, E32, ctl + CTL_PR);
     ASC_CUDA(cudaGetLastError());
     uint32_t flag = 0;
@@ -2539,16 +2724,20 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
         return fail(ASC_ERR_INVALID, "asc_bfs_device_noalloc: malformed CSR (%s%s%s)",
                     flag & 1 ? "offsets must start at 0 and end at E; " : "",
                     flag & 2 ? "offsets decrease; " : "", flag & 4 ? "destination >= V" : "");
+    noalloc_huge_bits_kernel<<<fill, kBlock, 0, s>>>(d_row_offsets, V32, kNoAllocHuge, huge_bits, nwords);
 
     RegionArgs a;
     memset(&a, 0, sizeof(a));
     a.ptr = d_row_offsets;
     a.edges = d_col;
     a.val = d_levels;
-    a.bitmap = bitmap;
     a.visited = visited;
+    a.huge_bits = huge_bits;
     a.S = V32;  // the whole graph is device resident: one region
     a.V = V32;
+    a.dense_begin = 0;
+    a.dense_end = V32;
+    a.dense_div = 64;
     a.huge = kNoAllocHuge;
     a.seg_len = kNoAllocSeg;
     a.segcap_static = (uint32_t)kNoAllocMaxSegs;
@@ -2557,31 +2746,37 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     a.cnt_out = ctl;
     a.q_out = queue[0];
     a.seg_out = segs[0];
+    a.bitmap = bitmap[0];
     init_values_kernel<kBFS><<<fill, kBlock, 0, s>>>(d_levels, V32, source);
-    seed_kernel<<<1, kBlock, 0, s>>>(a, source, 0);
+    seed_bits_kernel<<<1, kBlock, 0, s>>>(a, source, 0, nwords);
+    build_frontier_kernel<<<fill, kBlock, 0, s>>>(a, bitmap[0], nwords);
     ASC_CUDA(cudaGetLastError());
-    uint32_t cnt[4] = {0, 0, 0, 0};
+    uint32_t cnt[CTL_BLOCK] = {0, 0, 0, 0, 0, 0, 0, 0};
     ASC_CUDA(cudaMemcpyAsync(cnt, ctl, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
     int parity = 0;
     int64_t iters = 0;
-    while (cnt[0] | cnt[2]) {
+    while (cnt[6] | cnt[7]) {
         if (++iters > (int64_t)V + 2) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %lld iterations",
                                                   (long long)iters);
         const int po = 1 - parity;
         ASC_CUDA(cudaMemsetAsync(ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
-        ASC_CUDA(cudaMemsetAsync(bitmap, 0, 4 * (V / 32 + 2), s));
+        ASC_CUDA(cudaMemsetAsync(bitmap[po], 0, 4 * (V / 32 + 2), s));
         a.region = 0;
         a.q_in = queue[parity];
         a.seg_in = segs[parity];
+        a.bitmap_in = bitmap[parity];
+        a.bitmap = bitmap[po];
         a.cnt_in = ctl + CTL_BLOCK * parity;
         a.cnt_out = ctl + CTL_BLOCK * po;
         a.q_out = queue[po];
         a.seg_out = segs[po];
         a.work = a.cnt_out + 4;
-        const uint64_t items = (uint64_t)cnt[2] + (cnt[0] + kBlock - 1) / kBlock;
+        const bool dense = cnt[6] > V32 / a.dense_div;
+        const uint64_t items = (uint64_t)cnt[2] + ((dense ? V32 : cnt[0]) + kBlock - 1) / kBlock;
         const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)sms * 4));
         expand_kernel<kBFS, 1><<<grid, kBlock, 0, s>>>(a);
+        build_frontier_kernel<<<fill, kBlock, 0, s>>>(a, bitmap[po], nwords);
         ASC_CUDA(cudaGetLastError());
         ASC_CUDA(cudaMemcpyAsync(cnt, a.cnt_out, sizeof(cnt), cudaMemcpyDeviceToHost, s));
         ASC_CUDA(cudaStreamSynchronize(s));

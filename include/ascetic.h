@@ -288,7 +288,7 @@ asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double
  * the BFS has finished on it.
  * Limits: V <= 1,048,576 and E <= 16,777,216; larger graphs return
  * ASC_ERR_BUDGET. The CSR is checked on the device first (ASC_ERR_INVALID).
- * Scratch: one fixed device array of about 9.3 MB in this library, held by
+ * Scratch: one fixed device array of about 9.6 MB in this library, held by
  * every GPU that loads it until the process exits; no cudaMalloc, cudaFree or
  * allocating library routine is called. The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current, so
