@@ -53,6 +53,11 @@ def parse():
                     help="profiling aid: time the steps with one launch per region (phase timing)")
     ap.add_argument("--batch", type=int, default=64,
                     help="sources of the multi-source leg (0 skips it)")
+    ap.add_argument("--serve", default="16,18,20,22",
+                    help="RMAT scales of the resident graphs of the serving leg ('' skips it); "
+                         "20,22,24,26 is the full serving configuration")
+    ap.add_argument("--serve-queries", type=int, default=400)
+    ap.add_argument("--serve-budget-gb", type=float, default=12.0)
     return ap.parse_args()
 
 
@@ -158,6 +163,95 @@ def reference_arm(args):
                                        "orc_relax_mt) on %d host threads" % (args.steps, threads)},
             "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def serve_leg(args):
+    """Serving: BFS/SSSP/CC/PR queries (mix 50/30/10/10, graph uniform, sources
+    uniform over vertices with out-degree > 0) against resident RMAT graphs
+    (edge factor 16, seeds 5.., weights uniform in [1,63], static region 25% of
+    edge bytes) under one device budget. The continuous-batching server against
+    the plain one-query-at-a-time FIFO engine on the same GPU: saturating load
+    (all queries submitted at once), then Poisson arrivals at swept rates."""
+    import ascetic_gb300 as A
+    scales = [int(x) for x in args.serve.split(",") if x]
+    rng = np.random.default_rng(12345)
+    graphs, cands, hosts = [], [], []
+    t0 = time.time()
+    for i, sc in enumerate(scales):
+        ptr, adj = A.rmat_csr(sc, 16, 5 + i, weights=(1, 63))
+        deg = np.diff(ptr)
+        cands.append(np.nonzero(deg > 0)[0])
+        graphs.append(A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=args.budget)))
+        hosts.append((ptr, adj) if sc <= 20 else None)
+        del ptr, adj
+    t_gen = time.time() - t0
+    std32 = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
+    plan = []
+    for _ in range(args.serve_queries):
+        gi = int(rng.integers(0, len(scales)))
+        r = rng.random()
+        if r < 0.5:
+            algo = "bfs"
+        elif r < 0.8:
+            algo = "sssp"
+        elif r < 0.9:
+            algo = "cc"
+        else:
+            algo = "pr"
+        src = int(rng.choice(cands[gi])) if algo in ("bfs", "sssp") else 0
+        plan.append((gi, algo, src))
+    budget = int(args.serve_budget_gb * 1e9)
+
+    def run(mode, rate=None, n=None):
+        todo = plan if n is None else plan[:n]
+        with A.Server(budget_bytes=budget, mode=mode) as srv:
+            ids = [srv.add_graph(g) for g in graphs]
+            arr = np.cumsum(rng.exponential(1.0 / rate, size=len(todo))) if rate else None
+            tick = []
+            t_start = time.perf_counter()
+            for k, (gi, algo, src) in enumerate(todo):
+                if arr is not None:
+                    delay = t_start + arr[k] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                tick.append(srv.submit(ids[gi], algo, src, params=std32 if algo == "pr" else None))
+            outs = [srv.wait(t) for t in tick]
+            st = srv.stats()
+        return st, outs
+
+    # warm-up (graph loops, batch state) then saturating load
+    run(A.SERVE_BATCHED, n=min(40, len(plan)))
+    run(A.SERVE_FIFO, n=min(8, len(plan)))
+    sb, outs_b = run(A.SERVE_BATCHED)
+    sf, outs_f = run(A.SERVE_FIFO)
+    # every served BFS/SSSP/CC value equals the plain engine's (bit for bit)
+    exact = True
+    for (gi, algo, src), (ob, _), (of, _) in zip(plan, outs_b, outs_f):
+        if algo != "pr" and not np.array_equal(ob, of):
+            exact = False
+            break
+    res = {"graphs_rmat_scales": scales, "queries": len(plan), "mix": "50% BFS / 30% SSSP / 10% CC / 10% PR (FP32)",
+           "budget_bytes": budget, "graph_build_s": round(t_gen, 1),
+           "batched": {"qps": round(sb["queries_per_s"], 2), "p50_ms": round(sb["p50_ms"], 2),
+                       "p99_ms": round(sb["p99_ms"], 2), "device_bytes": sb["device_bytes"]},
+           "plain_fifo": {"qps": round(sf["queries_per_s"], 2), "p50_ms": round(sf["p50_ms"], 2),
+                          "p99_ms": round(sf["p99_ms"], 2)},
+           "qps_speedup": round(sb["queries_per_s"] / sf["queries_per_s"], 2) if sf["queries_per_s"] else None,
+           "results_equal_plain_engine": bool(exact), "load": "saturating (all submitted at t=0)"}
+    sweep = []
+    cap = sf["queries_per_s"]
+    n_sweep = min(len(plan), 120)
+    for frac in (0.5, 0.9, 2.0):
+        rate = frac * cap
+        b, _ = run(A.SERVE_BATCHED, rate=rate, n=n_sweep)
+        f, _ = run(A.SERVE_FIFO, rate=rate, n=n_sweep)
+        sweep.append({"rate_qps": round(rate, 2), "batched_p50_ms": round(b["p50_ms"], 2),
+                      "batched_p99_ms": round(b["p99_ms"], 2), "fifo_p50_ms": round(f["p50_ms"], 2),
+                      "fifo_p99_ms": round(f["p99_ms"], 2), "queries": n_sweep})
+    res["poisson_sweep"] = sweep
+    for g in graphs:
+        g.close()
+    return res
 
 
 def workload_config(args):
@@ -310,6 +404,9 @@ def main():
             extra["cc_iterations"] = st["iterations"]
         del sp, sc
         line["other_algorithms"] = extra
+
+    if args.serve:
+        line["serving"] = serve_leg(args)
 
     if not args.no_cpu:
         import oracle
