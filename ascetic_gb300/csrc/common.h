@@ -11,6 +11,8 @@
 
 namespace asc {
 
+struct BatchEngine;
+
 // Thread-local last-error message (asc_last_error).
 void set_error(const char *fmt, ...);
 asc_status fail(asc_status s, const char *fmt, ...);
@@ -60,12 +62,7 @@ struct Workspace {
     uint32_t n_huge_static = 0, n_huge_total = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> phase_events;
-    // multi-source batches (up to 64 sources of one graph)
-    unsigned long long *ms_visit = nullptr, *ms_front = nullptr, *ms_next = nullptr;  // u64 [V]
-    uint32_t *ms_touched = nullptr;  // vertices whose next mask went non-zero this iteration [V]
-    uint32_t *ms_out = nullptr;      // per-source values, [n][V] (or vertex-major [V][64] distances)
-    uint32_t *ms_dist = nullptr;     // batched SSSP distances, vertex-major [V][64]
-    uint32_t ms_out_n = 0;
+    struct BatchEngine *batch[2] = {nullptr, nullptr};  // asc_run_batch engines (BFS, SSSP)
     cudaGraphExec_t loop_exec[3] = {nullptr, nullptr, nullptr};  // BFS, SSSP, CC iteration loops
     uint32_t loop_cap[3] = {0, 0, 0};
     Tuning tune;
@@ -107,7 +104,6 @@ asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint3
                      void *out, asc_stats *st);
 void free_workspace(asc_graph *g);
 // continuous multi-source batches (engine.cu)
-struct BatchEngine;
 uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride);
 uint64_t batch_plane_bytes(asc_graph *g);
 asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **out);
@@ -117,7 +113,7 @@ asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source);
 bool batch_busy(const BatchEngine *b);
 asc_status batch_launch(BatchEngine *b);
 asc_status batch_collect(BatchEngine *b, uint64_t *finished);
-asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *host_out);
+asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *out, bool device_out);
 uint64_t workspace_bytes(asc_graph *g, bool pagerank);
 // graph.cpp
 asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t param_size);

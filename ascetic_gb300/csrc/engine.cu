@@ -1106,9 +1106,6 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 }  // namespace
 
 void free_ws_buffers(Workspace *ws) {
-    for (void *p : {(void *)ws->ms_visit, (void *)ws->ms_front, (void *)ws->ms_next, (void *)ws->ms_touched,
-                    (void *)ws->ms_out, (void *)ws->ms_dist})
-        if (p) cudaFree(p);
     for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->bitmap[0],
                     (void *)ws->bitmap[1],
                     (void *)ws->queue[0],
@@ -1127,6 +1124,11 @@ void free_ws_buffers(Workspace *ws) {
 void free_workspace(asc_graph *g) {
     Workspace *ws = g->ws;
     if (!ws) return;
+    for (auto &b : ws->batch)
+        if (b) {
+            batch_destroy(b);
+            b = nullptr;
+        }
     free_ws_buffers(ws);
     delete ws;
     g->ws = nullptr;
@@ -1397,30 +1399,56 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
 
 // -------------------------------------------- multi-source batches (<= 64) --
 //
-// Up to 64 BFS or SSSP queries of one graph advance together: each vertex
+// Up to 64 BFS or SSSP sources of one graph advance together: each vertex
 // carries a 64-bit mask of the sources for which it is in the frontier, so one
 // read of an edge serves every source of the batch. BFS keeps 64-bit visited /
 // frontier / next masks per vertex and is level-synchronous, so each source's
 // levels equal a single-source BFS from it. Batched SSSP keeps a vertex-major
 // [V][64] distance block (one 256-byte row per vertex) and relaxes the sources
 // of a frontier vertex's mask lane by lane; its fixpoint per source is the
-// single-source one. The frontier lists, segments and the static/on-demand
-// split are the single-query engine's.
+// single-source one. Expansion only ORs masks and marks touched vertices in a
+// bitmap; an apply pass over the touched words turns them into the next
+// frontier bitmap, and the compaction kernel of the single-query engine builds
+// the lists and segments.
+//
+// Batches are continuous: source slots are filled and emptied between
+// iterations. A query joins as soon as a slot (and, for BFS, a level plane) is
+// free, advances with the other sources, and leaves when its own frontier is
+// empty; levels are counted from the iteration the source joined, so every
+// query's values equal a solo run. asc_run_batch is one fill of the slots.
+struct BatchEngine {
+    asc_graph *g = nullptr;
+    bool sssp = false;
+    uint32_t stride = 64;             // SSSP distance row length (sources per row)
+    Workspace ws;                     // own frontier lists, bitmaps, counters
+    unsigned long long *visit = nullptr, *front = nullptr, *next = nullptr;
+    uint32_t *touched = nullptr;      // bitmap of vertices whose next mask went non-zero
+    uint32_t *dist = nullptr;         // SSSP [V][stride]
+    uint32_t *plane[64] = {nullptr};  // BFS per-slot level planes [V]
+    uint32_t **d_plane = nullptr;     // device copy of plane[]
+    int32_t *d_lvl_off = nullptr;     // per-slot level offset (level = iteration + offset)
+    int32_t lvl_off[64] = {0};
+    uint32_t *staging = nullptr;      // SSSP column gather [V]
+    cudaStream_t stream = nullptr;
+    int parity = 0;
+    uint32_t it = 0;                  // iterations run so far
+    uint64_t active = 0;              // slots in use
+    uint32_t pend_n = 0, pend_slot[64], pend_src[64];
+};
+
 namespace {
 
 constexpr int kMaxBatch = 64;
+enum { CTL_ALIVE = 34 };  // u64 (words 34-35): OR of the new frontier masks of an iteration
 
 struct MsArgs {
-    RegionArgs r0, r1;            // frontier lists/segments of both regions (val unused)
+    RegionArgs r0, r1;            // frontier lists/segments/bitmaps of both regions (val unused)
     unsigned long long *visit;    // BFS: sources that reached v
     unsigned long long *front;    // sources for which v is in the current frontier
     unsigned long long *next;     // sources that reached v in this iteration (atomicOr)
-    uint32_t *touched;            // vertices whose next mask went non-zero
-    uint32_t *touched_cnt;
+    uint32_t *touched;            // bitmap: v's next mask went non-zero this iteration
     uint32_t *work;
     uint32_t *dist;               // SSSP: [V][64]
-    uint32_t *levels;             // BFS: [n][V]
-    uint32_t n;                   // sources in the batch
     uint32_t V;
 };
 
@@ -1432,22 +1460,16 @@ struct MsSmem {
     uint32_t work;
 };
 
-__device__ __forceinline__ void push_touched(const MsArgs &m, bool won, uint32_t v) {
-    const unsigned msk = __ballot_sync(kFull, won);
-    if (!msk) return;
-    const int lane = threadIdx.x & 31, l = __ffs(msk) - 1;
-    uint32_t base = 0;
-    if (lane == l) base = atomicAdd(m.touched_cnt, (uint32_t)__popc(msk));
-    base = __shfl_sync(kFull, base, l);
-    if (won) m.touched[base + __popc(msk & ((1u << lane) - 1u))] = v;
-}
-
 // BFS relaxation of one edge for a whole mask: true when v's next mask was empty.
 __device__ __forceinline__ bool ms_reach(const MsArgs &m, uint32_t v, unsigned long long f,
                                          unsigned long long vis) {
     const unsigned long long nb = f & ~vis;
     if (!nb) return false;
     return atomicOr(&m.next[v], nb) == 0ull;
+}
+
+__device__ __forceinline__ void mark_touched(const MsArgs &m, bool first, uint32_t v) {
+    if (first) atomicOr(&m.touched[v >> 5], 1u << (v & 31));
 }
 
 template <int WORDS>
@@ -1505,7 +1527,7 @@ __device__ void ms_tile(const MsArgs &m, const RegionArgs &a, uint32_t tile, uin
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) vis[k] = fk[k] ? m.visit[v[k]] : ~0ull;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_touched(m, ms_reach(m, v[k], fk[k], vis[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) mark_touched(m, ms_reach(m, v[k], fk[k], vis[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -1535,7 +1557,7 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) push_touched(m, ok[k] && ms_reach(m, v[k], f, vis[k]), v[k]);
+        for (int k = 0; k < kUnroll; k++) mark_touched(m, ok[k] && ms_reach(m, v[k], f, vis[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
@@ -1548,8 +1570,8 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
     __shared__ MsSmem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
     int m0, m1;
-    region_items(m.r0, n0, s0, i0, m0);
-    region_items(m.r1, n1, s1, i1, m1);
+    region_items_bits(m.r0, n0, s0, i0, m0);
+    region_items_bits(m.r1, n1, s1, i1, m1);
     const uint32_t mm = min(i0, i1), total = i0 + i1;
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(m.work, 1u);
@@ -1573,74 +1595,6 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
             if (local < s0) ms_segment<WORDS>(m, m.r0, m.r0.seg_in[local]);
             else ms_tile<WORDS>(m, m.r0, local - s0, n0, m0, sm);
         }
-    }
-}
-
-// After the expansion: the new sources of each touched vertex become its
-// frontier mask, BFS levels are written, and the vertex joins the next lists.
-template <bool BFS>
-__global__ void ms_apply_kernel(MsArgs m, uint32_t level) {
-    const uint32_t n = *m.touched_cnt;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (i < n) {
-            v = m.touched[i];
-            unsigned long long nb = m.next[v];
-            m.next[v] = 0;
-            if (BFS) {
-                nb &= ~m.visit[v];
-                m.visit[v] |= nb;
-                unsigned long long t = nb;
-                while (t) {
-                    const int s = __ffsll((long long)t) - 1;
-                    t &= t - 1;
-                    m.levels[(uint64_t)s * m.V + v] = level;
-                }
-            }
-            m.front[v] = nb;
-            won = nb != 0;
-            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
-        }
-        push_warp(m.r0, won, v);
-    }
-}
-
-__global__ void ms_init_kernel(MsArgs m, const uint32_t *sources, uint32_t fill, uint32_t sssp) {
-    const uint64_t total = sssp ? (uint64_t)m.V * kMaxBatch : (uint64_t)m.n * m.V;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-        if (sssp) m.dist[i] = fill;
-        else m.levels[i] = fill;
-    }
-    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m.V; v += stride) {
-        if (!sssp) m.visit[v] = 0;
-        m.front[v] = 0;
-        m.next[v] = 0;
-    }
-}
-
-// Marks each source in its vertex's masks (duplicates share one frontier
-// entry) and pushes the distinct source vertices into the first frontier.
-__global__ void ms_seed_kernel(MsArgs m, const uint32_t *sources, uint32_t sssp) {
-    for (uint32_t base = 0; base < kMaxBatch; base += 32) {
-        const uint32_t i = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (i < m.n) {
-            v = sources[i];
-            const unsigned long long bit = 1ull << i;
-            if (sssp) m.dist[(uint64_t)v * kMaxBatch + i] = 1;
-            else {
-                atomicOr(&m.visit[v], bit);
-                m.levels[(uint64_t)i * m.V + v] = 1;
-            }
-            won = atomicOr(&m.front[v], bit) == 0ull;
-            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
-        }
-        push_warp(m.r0, won, v);
     }
 }
 
@@ -1678,11 +1632,8 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
                 if (nd < row[lane + 32]) imp_hi = nd < atomicMin(&row[lane + 32], nd);
             }
             const unsigned blo = __ballot_sync(kFull, imp_lo), bhi = __ballot_sync(kFull, imp_hi);
-            if (blo | bhi) {
-                bool won = false;
-                if (lane == 0) won = atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull;
-                push_touched(m, won, v);
-            }
+            if ((blo | bhi) && lane == 0)
+                mark_touched(m, atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull, v);
         }
     }
 }
@@ -1711,7 +1662,8 @@ __device__ __forceinline__ void ms_sssp_item(const MsArgs &m, const RegionArgs &
 }
 
 // Work items are per warp and handed out 8 at a time: [static segments and
-// list vertices][on-demand segments and list vertices].
+// list vertices][on-demand segments and list vertices]. The SSSP batch always
+// builds lists (its RegionArgs carry dense_div = 0).
 __global__ void __launch_bounds__(kBlock) ms_sssp_expand_kernel(MsArgs m) {
     const uint32_t n0 = m.r0.cnt_in[0], s0 = m.r0.cnt_in[2];
     const uint32_t n1 = m.r1.cnt_in[1], s1 = m.r1.cnt_in[3];
@@ -1731,243 +1683,26 @@ __global__ void __launch_bounds__(kBlock) ms_sssp_expand_kernel(MsArgs m) {
     }
 }
 
-// [V][64] distances -> [n][V] per-source rows (32x32 tiles through shared memory).
-__global__ void ms_transpose_kernel(const uint32_t *dist, uint32_t *out, uint32_t V, uint32_t n) {
-    __shared__ uint32_t t[32][33];
-    const uint32_t v0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
-    for (uint32_t r = threadIdx.y; r < 32; r += blockDim.y) {
-        const uint32_t v = v0 + r, s = s0 + threadIdx.x;
-        t[r][threadIdx.x] = v < V ? dist[(uint64_t)v * kMaxBatch + s] : 0;
-    }
-    __syncthreads();
-    for (uint32_t r = threadIdx.y; r < 32; r += blockDim.y) {
-        const uint32_t s = s0 + r, v = v0 + threadIdx.x;
-        if (s < n && v < V) out[(uint64_t)s * V + v] = t[threadIdx.x][r];
-    }
-}
-
-}  // namespace
-
-asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params &p,
-                     void *out, asc_stats *st) {
-    ASC_TRY(ensure_workspace(g));
-    Workspace *ws = g->ws;
-    const uint32_t V = (uint32_t)g->V;
-    const bool sssp = algo == ASC_SSSP;
-    cudaStream_t s = g->stream;
-    if (!ws->ms_visit) {
-        ASC_CUDA(cudaMalloc(&ws->ms_visit, 8ull * V));
-        ASC_CUDA(cudaMalloc(&ws->ms_front, 8ull * V));
-        ASC_CUDA(cudaMalloc(&ws->ms_next, 8ull * V));
-        ASC_CUDA(cudaMalloc(&ws->ms_touched, 4ull * V));
-        ws->device_bytes += 28ull * V;
-    }
-    if (sssp && !ws->ms_dist) {
-        ASC_CUDA(cudaMalloc(&ws->ms_dist, 4ull * V * kMaxBatch));
-        ws->device_bytes += 4ull * V * kMaxBatch;
-    }
-    if (ws->ms_out_n < n) {
-        if (ws->ms_out) {
-            cudaFree(ws->ms_out);
-            ws->device_bytes -= 4ull * V * ws->ms_out_n;
-        }
-        ws->ms_out = nullptr;
-        ws->ms_out_n = 0;
-        ASC_CUDA(cudaMalloc(&ws->ms_out, 4ull * V * n));
-        ws->ms_out_n = n;
-        ws->device_bytes += 4ull * V * n;
-    }
-    uint32_t *d_src = ws->queue[1];  // the sources ride in the parity-1 list, unused until iteration 1
-    MsArgs m;
-    memset(&m, 0, sizeof(m));
-    m.visit = ws->ms_visit;
-    m.front = ws->ms_front;
-    m.next = ws->ms_next;
-    m.touched = ws->ms_touched;
-    m.dist = ws->ms_dist;
-    m.levels = ws->ms_out;
-    m.n = n;
-    m.V = V;
-    uint32_t launches = 0;
-
-    ASC_CUDA(cudaEventRecord(ws->ev[0], s));
-    ASC_CUDA(cudaMemcpyAsync(d_src, sources, 4ull * n, cudaMemcpyHostToDevice, s));
-    ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
-    for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(ws->bitmap[i], 0, 4 * (V / 32 + 2), s));
-    ms_init_kernel<<<fill_grid(ws, (uint64_t)V * (sssp ? kMaxBatch : n)), kBlock, 0, s>>>(m, d_src, V + 1,
-                                                                                           sssp ? 1 : 0);
-    m.r0 = base_args(g, 1);  // seeds land in parity 0
-    ms_seed_kernel<<<1, 32, 0, s>>>(m, d_src, sssp ? 1 : 0);
-    launches += 2;
-    ASC_CUDA(cudaGetLastError());
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 16, cudaMemcpyDeviceToHost, s));
-    ASC_CUDA(cudaStreamSynchronize(s));
-    uint32_t cnt[4];
-    memcpy(cnt, ws->h_ctl, sizeof(cnt));
-    int parity = 0, iters = 0;
-    const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
-    uint32_t *touched_cnt = ws->ctl + CTL_PR;  // word 32: free outside PageRank
-    const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
-    while (cnt[0] | cnt[1] | cnt[2] | cnt[3]) {
-        if (iters >= cap) return fail(ASC_ERR_TIMEOUT, "batch has no fixpoint after %d iterations", iters);
-        iters++;
-        const int po = 1 - parity;
-        ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
-        ASC_CUDA(cudaMemsetAsync(touched_cnt, 0, 4, s));
-        ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
-        m.r0 = region_args(g, parity, 0, false);
-        m.r1 = region_args(g, parity, 1, false);
-        m.work = m.r0.cnt_out + 4;
-        m.touched_cnt = touched_cnt;
-        if (sssp) ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
-        else if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
-        else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
-        if (sssp) ms_apply_kernel<false><<<grid, kBlock, 0, s>>>(m, 0);
-        else ms_apply_kernel<true><<<grid, kBlock, 0, s>>>(m, (uint32_t)iters + 1);
-        launches += 2;
-        ASC_CUDA(cudaGetLastError());
-        ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 16, cudaMemcpyDeviceToHost, s));
-        ASC_CUDA(cudaStreamSynchronize(s));
-        memcpy(cnt, ws->h_ctl, sizeof(cnt));
-        parity = po;
-    }
-    if (sssp) {
-        dim3 tg((V + 31) / 32, (n + 31) / 32);
-        ms_transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(ws->ms_dist, ws->ms_out, V, n);
-        launches++;
-    }
-    ASC_CUDA(cudaEventRecord(ws->ev[1], s));
-    ASC_CUDA(cudaGetLastError());
-    if (out && !(p.flags & ASC_RUN_NO_OUTPUT))
-        ASC_CUDA(cudaMemcpyAsync(out, ws->ms_out, 4ull * V * n,
-                                 (p.flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                 s));
-    ASC_CUDA(cudaEventRecord(ws->ev[2], s));
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 6, cudaMemcpyDeviceToHost, s));
-    ASC_CUDA(cudaStreamSynchronize(s));
-    if (st) {
-        memset(st, 0, sizeof(*st));
-        const unsigned long long *hs = (const unsigned long long *)(ws->h_ctl + CTL_STATS);
-        st->iterations = iters;
-        st->edges_processed = hs[0] + hs[1];
-        st->ondemand_edges = hs[1];
-        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
-        st->frontier_vertices = hs[2] + hs[3];
-        st->ondemand_vertices = hs[3];
-        float ms = 0;
-        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[0], ws->ev[1]));
-        st->ms_total = ms;
-        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[1], ws->ev[2]));
-        st->ms_copyout = ms;
-        st->kernel_launches = launches;
-    }
-    return ASC_OK;
-}
-
-// ------------------------------------------- continuous multi-source batches --
-//
-// The serving loop keeps one batch per (graph, BFS | SSSP) whose 64 source
-// slots are filled and emptied between iterations: a query joins the running
-// batch as soon as a slot (and, for BFS, a level plane) is free, advances with
-// the other sources in shared iterations, and leaves when its own frontier is
-// empty. Levels are written relative to the iteration the source joined, so
-// every query's values equal a solo run from its source.
-struct BatchEngine {
-    asc_graph *g = nullptr;
-    bool sssp = false;
-    uint32_t stride = 64;             // SSSP distance row length (sources per row)
-    Workspace ws;                     // own frontier lists, bitmaps, counters
-    unsigned long long *visit = nullptr, *front = nullptr, *next = nullptr;
-    uint32_t *touched = nullptr;
-    uint32_t *dist = nullptr;         // SSSP [V][stride]
-    uint32_t *plane[64] = {nullptr};  // BFS per-slot level planes [V]
-    uint32_t **d_plane = nullptr;     // device copy of plane[]
-    int32_t *d_lvl_off = nullptr;     // per-slot level offset (level = iteration + offset)
-    int32_t lvl_off[64] = {0};
-    uint32_t *staging = nullptr;      // SSSP column gather [V]
-    cudaStream_t stream = nullptr;
-    int parity = 0;
-    uint32_t it = 0;                  // iterations run so far
-    uint64_t active = 0;              // slots in use
-    uint64_t joined_since_step = 0;   // slots admitted before the next iteration
-    uint32_t pend_n = 0, pend_slot[64], pend_src[64];
-    uint64_t bytes = 0;
-    uint32_t cnt[4] = {0, 0, 0, 0};
-};
-
-namespace {
-
-enum { CTL_ALIVE = 34 };  // u64 (words 34-35): OR of the new frontier masks of an iteration
-
-struct Admit {
-    uint32_t n;
-    uint32_t slot[64];
-    uint32_t src[64];
-};
-
-// Resets the per-slot state of newly admitted slots: BFS clears their bits in
-// every visited mask and fills their level planes, SSSP resets their distance
-// columns.
-__global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint32_t stride, uint32_t **planes,
-                                unsigned long long newmask, uint32_t V, uint32_t fill, uint32_t sssp) {
-    const uint64_t n = (uint64_t)V;
-    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        unsigned long long t = newmask;
-        if (!sssp) visit[v] &= ~newmask;
-        while (t) {
-            const int s = __ffsll((long long)t) - 1;
-            t &= t - 1;
-            if (sssp) dist[v * stride + s] = fill;
-            else planes[s][v] = fill;
-        }
-    }
-}
-
-// Admission, phase 1: a new source that is not in the current frontier gets a
-// fresh frontier mask (front[] of non-members may hold stale bits).
-__global__ void cb_admit_reset_kernel(Admit ad, unsigned long long *front, const uint32_t *bitmap_in) {
-    const uint32_t i = threadIdx.x;
-    if (i < ad.n) {
-        const uint32_t v = ad.src[i];
-        if (!((bitmap_in[v >> 5] >> (v & 31)) & 1u)) front[v] = 0;
-    }
-}
-
-// Admission, phase 2: mark each source at level / distance 1 and add it to the
-// current frontier (pushing the vertex when it was not a member yet).
-__global__ void cb_admit_kernel(Admit ad, MsArgs m, uint32_t **planes, uint32_t stride, uint32_t sssp) {
-    for (uint32_t base = 0; base < 64; base += 32) {
-        const uint32_t i = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (i < ad.n) {
-            const uint32_t s = ad.slot[i];
-            v = ad.src[i];
-            const unsigned long long bit = 1ull << s;
-            if (sssp) m.dist[(uint64_t)v * stride + s] = 1;
-            else {
-                atomicOr(&m.visit[v], bit);
-                planes[s][v] = 1;
-            }
-            atomicOr(&m.front[v], bit);
-            won = !(atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31)) & (1u << (v & 31)));
-        }
-        push_warp(m.r0, won, v);
-    }
-}
-
+// Apply pass (one thread per word of the touched bitmap): the new sources of a
+// touched vertex become its frontier mask, BFS levels are written into the
+// sources' planes, and the vertex's bit goes into the next frontier bitmap
+// (with per-region counts for the compaction kernel). ORs every new mask into
+// *alive so finished sources can be told apart.
 template <bool BFS>
-__global__ void cb_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_off, uint32_t it,
-                                unsigned long long *alive) {
-    const uint32_t n = *m.touched_cnt;
-    const uint32_t stride = gridDim.x * blockDim.x;
+__global__ void ms_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_off, uint32_t it,
+                                unsigned long long *alive, uint32_t nwords) {
+    const RegionArgs &a = m.r0;
     unsigned long long any = 0;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        bool won = false;
-        uint32_t v = 0;
-        if (i < n) {
-            v = m.touched[i];
+    uint32_t n0 = 0, n1 = 0;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        uint32_t word = m.touched[w];
+        if (!word) continue;
+        m.touched[w] = 0;
+        uint32_t nbits = 0;
+        while (word) {
+            const int b = __ffs(word) - 1;
+            word &= word - 1;
+            const uint32_t v = 32 * w + b;
             unsigned long long nb = m.next[v];
             m.next[v] = 0;
             if (BFS) {
@@ -1982,14 +1717,92 @@ __global__ void cb_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_
             }
             m.front[v] = nb;
             any |= nb;
-            won = nb != 0;
-            if (won) atomicOr(&m.r0.bitmap[v >> 5], 1u << (v & 31));
+            if (nb) nbits |= 1u << b;
         }
-        push_warp(m.r0, won, v);
+        if (nbits) {
+            a.bitmap[w] = nbits;
+            const uint32_t v0 = 32 * w;
+            const uint32_t smask = v0 + 32 <= a.S ? 0xffffffffu : (v0 >= a.S ? 0 : (1u << (a.S - v0)) - 1u);
+            n0 += __popc(nbits & smask);
+            n1 += __popc(nbits & ~smask);
+        }
     }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) any |= __shfl_down_sync(kFull, any, d);
-    if ((threadIdx.x & 31) == 0 && any) atomicOr(alive, any);
+    for (int d = 16; d > 0; d >>= 1) {
+        any |= __shfl_down_sync(kFull, any, d);
+        n0 += __shfl_down_sync(kFull, n0, d);
+        n1 += __shfl_down_sync(kFull, n1, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (any) atomicOr(alive, any);
+        if (n0) atomicAdd(&a.cnt_out[6], n0);
+        if (n1) atomicAdd(&a.cnt_out[7], n1);
+    }
+}
+
+struct Admit {
+    uint32_t n;
+    uint32_t slot[64];
+    uint32_t src[64];
+};
+
+// Resets the per-slot state of newly admitted slots: BFS clears their bits in
+// every visited mask and fills their level planes, SSSP resets their distance
+// columns.
+__global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint32_t stride, uint32_t **planes,
+                                unsigned long long newmask, uint32_t V, uint32_t fill, uint32_t sssp) {
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
+        unsigned long long t = newmask;
+        if (!sssp) visit[v] &= ~newmask;
+        while (t) {
+            const int s = __ffsll((long long)t) - 1;
+            t &= t - 1;
+            if (sssp) dist[v * stride + s] = fill;
+            else planes[s][v] = fill;
+        }
+    }
+}
+
+// Admission, phase 1: a new source that is not in the current frontier gets a
+// fresh frontier mask (front[] of non-members may hold stale bits).
+__global__ void cb_admit_reset_kernel(Admit ad, unsigned long long *front, const uint32_t *bitmap_cur) {
+    const uint32_t i = threadIdx.x;
+    if (i < ad.n) {
+        const uint32_t v = ad.src[i];
+        if (!((bitmap_cur[v >> 5] >> (v & 31)) & 1u)) front[v] = 0;
+    }
+}
+
+// Admission, phase 2: marks each source at level / distance 1 and adds it to
+// the current frontier: a vertex that was not a member gets its bit and its
+// region count, and joins its region list (or, for a long list, the segment
+// list). A region walked through its bitmap ignores the list.
+__global__ void cb_admit_kernel(Admit ad, MsArgs m, RegionArgs cur, uint32_t **planes, uint32_t stride,
+                                uint32_t sssp) {
+    const uint32_t i = threadIdx.x;
+    if (i >= ad.n) return;
+    const uint32_t s = ad.slot[i], v = ad.src[i];
+    const unsigned long long bit = 1ull << s;
+    if (sssp) m.dist[(uint64_t)v * stride + s] = 1;
+    else {
+        atomicOr(&m.visit[v], bit);
+        planes[s][v] = 1;
+    }
+    atomicOr(&m.front[v], bit);
+    const uint32_t vb = 1u << (v & 31);
+    if (atomicOr(&cur.bitmap[v >> 5], vb) & vb) return;  // already in the frontier
+    const bool od = v >= cur.S;
+    atomicAdd(&cur.cnt_out[6 + od], 1u);
+    const uint32_t deg = cur.ptr[v + 1] - cur.ptr[v];
+    if (deg > cur.huge) {
+        const uint32_t nseg = (deg + cur.seg_len - 1) / cur.seg_len;
+        const uint32_t sb = atomicAdd(&cur.cnt_out[2 + od], nseg);
+        uint64_t *dst = cur.seg_out + (od ? cur.segcap_static : 0) + sb;
+        for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
+    } else {
+        const uint32_t pos = atomicAdd(&cur.cnt_out[od], 1u);
+        cur.q_out[(od ? cur.S : 0) + pos] = v;
+    }
 }
 
 __global__ void cb_gather_column_kernel(const uint32_t *dist, uint32_t stride, uint32_t s, uint32_t *out, uint32_t V) {
@@ -2001,7 +1814,7 @@ __global__ void cb_gather_column_kernel(const uint32_t *dist, uint32_t stride, u
 
 uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride) {
     const uint64_t V = g->V;
-    uint64_t b = 28 * V + 16 * V + 3 * 4 * (V / 32 + 2) + 1024;  // masks, touched, lists, bitmaps
+    uint64_t b = 24 * V + 4 * (V / 32 + 2) + 16 * V + 4 * 4 * (V / 32 + 2) + 8 * (g->E / 256 + 1024) + 4096;
     if (sssp) b += 4ull * V * stride + 4 * V;
     return b;
 }
@@ -2012,7 +1825,7 @@ uint64_t batch_plane_bytes(asc_graph *g) { return 4ull * g->V; }
 // run; exact afterwards), with the PageRank buffers when asked for.
 uint64_t workspace_bytes(asc_graph *g, bool pagerank) {
     const uint64_t V = g->V;
-    uint64_t b = g->ws ? g->ws->device_bytes : 4 * V + 3 * 4 * (V / 32 + 2) + 8 * V + 8 * (g->E / 256 + 1024) + 4096;
+    uint64_t b = g->ws ? g->ws->device_bytes : 4 * V + 4 * 4 * (V / 32 + 2) + 8 * V + 8 * (g->E / 256 + 1024) + 4096;
     if (pagerank && (!g->ws || !g->ws->pr_rank)) b += 4ull * 8 * V;
     return b;
 }
@@ -2035,7 +1848,9 @@ asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **
     b->g = g;
     b->sssp = sssp;
     b->stride = stride;
-    asc_status st = alloc_workspace(g, &b->ws);
+    asc_status st = stride == 64 ? ASC_OK : fail(ASC_ERR_UNSUPPORTED, "batch rows of %u sources", stride);
+    if (st == ASC_OK) st = alloc_workspace(g, &b->ws);
+    if (sssp) b->ws.tune.dense_div = 0;  // the SSSP batch walks lists only
     const uint64_t V = g->V;
     auto al = [&](void **p, size_t n) {
         if (st != ASC_OK) return;
@@ -2045,7 +1860,7 @@ asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **
     al((void **)&b->visit, 8 * V);
     al((void **)&b->front, 8 * V);
     al((void **)&b->next, 8 * V);
-    al((void **)&b->touched, 4 * V);
+    al((void **)&b->touched, 4 * (V / 32 + 2));
     al((void **)&b->d_plane, 8 * 64);
     al((void **)&b->d_lvl_off, 4 * 64);
     if (sssp) {
@@ -2058,10 +1873,10 @@ asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **
     }
     // empty start state: no frontier, zero masks
     if (st == ASC_OK) {
-        cudaError_t e = cudaSuccess;
-        if (e == cudaSuccess) e = cudaMemsetAsync(b->ws.ctl, 0, 4 * CTL_WORDS, b->stream);
+        cudaError_t e = cudaMemsetAsync(b->ws.ctl, 0, 4 * CTL_WORDS, b->stream);
         for (int i = 0; i < 2 && e == cudaSuccess; i++)
             e = cudaMemsetAsync(b->ws.bitmap[i], 0, 4 * (V / 32 + 2), b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->touched, 0, 4 * (V / 32 + 2), b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->visit, 0, 8 * V, b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->front, 0, 8 * V, b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(b->next, 0, 8 * V, b->stream);
@@ -2090,7 +1905,6 @@ asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source) {
     b->pend_src[b->pend_n] = source;
     b->pend_n++;
     b->active |= 1ull << slot;
-    b->joined_since_step |= 1ull << slot;
     return ASC_OK;
 }
 
@@ -2103,6 +1917,7 @@ asc_status batch_launch(BatchEngine *b) {
     Workspace *ws = &b->ws;
     cudaStream_t s = b->stream;
     const uint32_t V = (uint32_t)g->V;
+    const uint32_t nwords = V / 32 + 1;
     const int p = b->parity, po = 1 - p;
     MsArgs m;
     memset(&m, 0, sizeof(m));
@@ -2112,7 +1927,6 @@ asc_status batch_launch(BatchEngine *b) {
     m.touched = b->touched;
     m.dist = b->dist;
     m.V = V;
-    m.n = 64;
     if (b->pend_n) {
         Admit ad;
         memset(&ad, 0, sizeof(ad));
@@ -2127,38 +1941,30 @@ asc_status batch_launch(BatchEngine *b) {
         ASC_CUDA(cudaMemcpyAsync(b->d_lvl_off, b->lvl_off, 4 * 64, cudaMemcpyHostToDevice, s));
         cb_clear_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(b->visit, b->dist, b->stride, b->d_plane, newmask, V, V + 1,
                                                              b->sssp ? 1 : 0);
-        RegionArgs in = base_args(g, ws, 1 - p);  // writes into the lists of parity p (this iteration's input)
+        RegionArgs cur = base_args(g, ws, 1 - p);  // the lists/bitmap/counts of parity p (this iteration's input)
         cb_admit_reset_kernel<<<1, 64, 0, s>>>(ad, b->front, ws->bitmap[p]);
-        m.r0 = in;
-        cb_admit_kernel<<<1, 32, 0, s>>>(ad, m, b->d_plane, b->stride, b->sssp ? 1 : 0);
+        cb_admit_kernel<<<1, 64, 0, s>>>(ad, m, cur, b->d_plane, b->stride, b->sssp ? 1 : 0);
         ASC_CUDA(cudaGetLastError());
         b->pend_n = 0;
     }
-    b->joined_since_step = 0;
-    uint32_t *touched_cnt = ws->ctl + CTL_PR;
     unsigned long long *alive = (unsigned long long *)(ws->ctl + CTL_ALIVE);
     ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
-    ASC_CUDA(cudaMemsetAsync(touched_cnt, 0, 4, s));
     ASC_CUDA(cudaMemsetAsync(alive, 0, 8, s));
     ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
     m.r0 = region_args(g, ws, p, 0, false);
     m.r1 = region_args(g, ws, p, 1, false);
     m.work = m.r0.cnt_out + 4;
-    m.touched_cnt = touched_cnt;
     const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
     b->it++;
-    if (b->sssp) {
-        if (b->stride != 64) return fail(ASC_ERR_UNSUPPORTED, "SSSP batch rows of %u sources", b->stride);
-        m.r0.dense_div = m.r1.dense_div = 0;
-        ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
-        cb_apply_kernel<false><<<grid, kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it, alive);
-    } else {
-        if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
-        else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
-        cb_apply_kernel<true><<<grid, kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it, alive);
-    }
+    if (b->sssp) ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
+    else if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
+    else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
+    if (b->sssp) ms_apply_kernel<false><<<fill_grid(ws, nwords), kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it,
+                                                                               alive, nwords);
+    else ms_apply_kernel<true><<<fill_grid(ws, nwords), kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it, alive,
+                                                                        nwords);
+    build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(m.r0, ws->bitmap[po], nwords);
     ASC_CUDA(cudaGetLastError());
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 16, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_ALIVE, alive, 8, cudaMemcpyDeviceToHost, s));
     b->parity = po;
     return ASC_OK;
@@ -2175,17 +1981,85 @@ asc_status batch_collect(BatchEngine *b, uint64_t *finished) {
     return ASC_OK;
 }
 
-// Copies a finished slot's values (V u32) to host memory.
-asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *host_out) {
+// Copies a finished slot's values (V u32) to host or device memory.
+asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *out, bool device_out = false) {
     const uint32_t V = (uint32_t)b->g->V;
+    const cudaMemcpyKind kind = device_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (b->sssp) {
         cb_gather_column_kernel<<<fill_grid(&b->ws, V), kBlock, 0, b->stream>>>(b->dist, b->stride, slot, b->staging, V);
         ASC_CUDA(cudaGetLastError());
-        ASC_CUDA(cudaMemcpyAsync(host_out, b->staging, 4ull * V, cudaMemcpyDeviceToHost, b->stream));
+        ASC_CUDA(cudaMemcpyAsync(out, b->staging, 4ull * V, kind, b->stream));
     } else {
-        ASC_CUDA(cudaMemcpyAsync(host_out, b->plane[slot], 4ull * V, cudaMemcpyDeviceToHost, b->stream));
+        ASC_CUDA(cudaMemcpyAsync(out, b->plane[slot], 4ull * V, kind, b->stream));
     }
     ASC_CUDA(cudaStreamSynchronize(b->stream));
+    return ASC_OK;
+}
+
+// asc_run_batch: all n sources fill slots 0..n-1 of the graph's own batch
+// engine (kept for later batches), then iterations run until every source is
+// done; each finished slot's values are copied to row i of out.
+asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, const asc_params &p,
+                     void *out, asc_stats *st) {
+    ASC_TRY(ensure_workspace(g));
+    Workspace *ws = g->ws;
+    const int k = algo == ASC_SSSP ? 1 : 0;
+    if (!ws->batch[k]) ASC_TRY(batch_create(g, k == 1, 64, &ws->batch[k]));
+    BatchEngine *b = ws->batch[k];
+    const uint32_t V = (uint32_t)g->V;
+    cudaStream_t s = b->stream;
+    ASC_CUDA(cudaMemsetAsync(b->ws.ctl + CTL_STATS, 0, 8 * 6, s));
+    ASC_CUDA(cudaEventRecord(ws->ev[0], s));
+    for (uint32_t i = 0; i < n; i++) ASC_TRY(batch_admit(b, i, sources[i]));
+    const uint32_t it0 = b->it;
+    const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
+    uint64_t done = 0;
+    const bool want = out && !(p.flags & ASC_RUN_NO_OUTPUT);
+    double copy_ms = 0;
+    while (b->active) {
+        if ((int64_t)(b->it - it0) >= cap) {
+            // drop the unfinished slots so the engine is reusable
+            b->active = 0;
+            return fail(ASC_ERR_TIMEOUT, "batch has no fixpoint after %u iterations", b->it - it0);
+        }
+        ASC_TRY(batch_launch(b));
+        uint64_t fin = 0;
+        ASC_TRY(batch_collect(b, &fin));
+        done |= fin;
+        if (want) {
+            cudaEvent_t e0 = ws->ev[2], e1 = ws->ev[3];
+            ASC_CUDA(cudaEventRecord(e0, s));
+            while (fin) {
+                const uint32_t slot = __builtin_ctzll(fin);
+                fin &= fin - 1;
+                ASC_TRY(batch_fetch(b, slot, (uint32_t *)out + (uint64_t)slot * V,
+                                    (p.flags & ASC_RUN_DEVICE_OUT) != 0));
+            }
+            ASC_CUDA(cudaEventRecord(e1, s));
+            ASC_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            ASC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            copy_ms += ms;
+        }
+    }
+    ASC_CUDA(cudaEventRecord(ws->ev[1], s));
+    ASC_CUDA(cudaMemcpyAsync(b->ws.h_ctl + CTL_STATS, b->ws.ctl + CTL_STATS, 8 * 6, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaStreamSynchronize(s));
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        const unsigned long long *hs = (const unsigned long long *)(b->ws.h_ctl + CTL_STATS);
+        st->iterations = (int32_t)(b->it - it0);
+        st->edges_processed = hs[0] + hs[1];
+        st->ondemand_edges = hs[1];
+        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->frontier_vertices = hs[2] + hs[3];
+        st->ondemand_vertices = hs[3];
+        float ms = 0;
+        ASC_CUDA(cudaEventElapsedTime(&ms, ws->ev[0], ws->ev[1]));
+        st->ms_total = ms - copy_ms;
+        st->ms_copyout = copy_ms;
+        st->kernel_launches = (uint32_t)(4 * (b->it - it0) + 3);
+    }
     return ASC_OK;
 }
 

@@ -242,7 +242,7 @@ void batch_loop(asc_server *s) {
                 Query *q = gs.slot_q[k][slot];
                 if (!q) continue;
                 asc_status st = sts[i];
-                if (st == ASC_OK && q->out) st = asc::batch_fetch(gs.batch[k], slot, q->out);
+                if (st == ASC_OK && q->out) st = asc::batch_fetch(gs.batch[k], slot, q->out, false);
                 q->batch = width;
                 done.push_back({q, st});
                 gs.slot_q[k][slot] = nullptr;
