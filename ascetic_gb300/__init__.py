@@ -41,7 +41,9 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_rmat_csr", "asc_graph_rmat", "asc_write_graph", "asc_link_probe",
             "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
             "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
-            "asc_server_stats_get", "asc_server_destroy"]
+            "asc_server_stats_get", "asc_server_destroy", "asc_graph_get_tuning", "asc_graph_set_tuning",
+            "asc_graph_tune"]
+TUNE_NO_CACHE = 1
 SERVE_BATCHED, SERVE_FIFO = 0, 1
 
 
@@ -65,6 +67,14 @@ class GraphInfo(ctypes.Structure):
                 ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
                 ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("huge_degree", ctypes.c_uint32), ("segment_edges", ctypes.c_uint32),
+                ("dense_div", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32), ("ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ServerConfig(ctypes.Structure):
@@ -152,6 +162,9 @@ def lib():
         "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
         "asc_run_batch": ([c_vp, ctypes.c_int, c_vp, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
         "asc_server_config_default": ([P(ServerConfig)], None),
+        "asc_graph_get_tuning": ([c_vp, P(Tuning)], ctypes.c_int),
+        "asc_graph_set_tuning": ([c_vp, P(Tuning)], ctypes.c_int),
+        "asc_graph_tune": ([c_vp, ctypes.c_int, c_vp, c_u32, c_u32, P(Tuning)], ctypes.c_int),
         "asc_server_create": ([P(ServerConfig), gpp], ctypes.c_int),
         "asc_server_add_graph": ([c_vp, c_vp, P(c_u32)], ctypes.c_int),
         "asc_server_submit": ([c_vp, c_u32, ctypes.c_int, c_u32, P(Params), c_vp, P(c_u64)], ctypes.c_int),
@@ -312,6 +325,33 @@ def _run_batch(self, algo, sources, params=None, out=None, no_output=False):
 
 
 Graph.run_batch = _run_batch
+
+
+def _tune(self, algo, sources=(), cache=True):
+    """Autotunes the engine's thresholds for this graph; returns the setting."""
+    if isinstance(algo, str):
+        algo = ALGOS[algo]
+    src = np.ascontiguousarray(list(sources) or [0], dtype=np.uint32)
+    t = Tuning()
+    _check(lib().asc_graph_tune(self._h, algo, src.ctypes.data, len(src), 0 if cache else TUNE_NO_CACHE,
+                                ctypes.byref(t)))
+    return t.as_dict()
+
+
+def _get_tuning(self):
+    t = Tuning()
+    _check(lib().asc_graph_get_tuning(self._h, ctypes.byref(t)))
+    return t.as_dict()
+
+
+def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0):
+    t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, 0.0)
+    _check(lib().asc_graph_set_tuning(self._h, ctypes.byref(t)))
+
+
+Graph.tune = _tune
+Graph.get_tuning = _get_tuning
+Graph.set_tuning = _set_tuning
 
 
 class Server:

@@ -93,6 +93,8 @@ struct asc_graph {
     cudaStream_t stream = nullptr;
     asc::Workspace *ws = nullptr;
     uint64_t device_vertex_bytes = 0;
+    bool has_tuning = false;      // tuning chosen by asc_graph_set_tuning / asc_graph_tune
+    asc::Tuning tuning;
 };
 
 namespace asc {

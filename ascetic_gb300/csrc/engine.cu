@@ -33,6 +33,8 @@
 
 #include <algorithm>
 #include <mutex>
+#include <string>
+#include <sys/stat.h>
 
 #include "common.h"
 
@@ -845,12 +847,14 @@ __global__ void seed_huge_segments_kernel(RegionArgs a, const uint32_t *huge_lis
 // Sizes and allocates the frontier machinery of one run for graph g.
 asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
     ws->V = g->V;
+    if (g->has_tuning) ws->tune = g->tuning;
     ASC_CUDA(cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, g->device));
     {
         // persistent grids fill the GPU: as many CTAs per SM as stay resident
         int per_sm = 0;
         ASC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, expand_fused_kernel<kSSSP, 2>, kBlock, 0));
-        ws->tune.ctas_per_sm = (uint32_t)std::max(1, per_sm);
+        const uint32_t resident = (uint32_t)std::max(1, per_sm);
+        if (!g->has_tuning || !ws->tune.ctas_per_sm || ws->tune.ctas_per_sm > resident) ws->tune.ctas_per_sm = resident;
     }
     const uint64_t V = g->V;
     const uint32_t S = g->static_vertices;
@@ -2658,3 +2662,183 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     }
     return ASC_OK;
 }
+
+// ------------------------------------------------------------- autotuner ----
+//
+// Picks the engine's tunables for one graph by measurement: the degree above
+// which a list is cut into segments, the segment length, the frontier density
+// above which a region is walked through its bitmap, and the CTAs per SM of
+// the persistent grids. Coordinate descent from the current setting, each
+// candidate timed over the given sources (CUDA events, best of two passes).
+// Results are cached in a text file keyed by GPU and graph shape
+// (ASC_TUNE_CACHE, default $HOME/.cache/ascetic_gb300_tune.txt).
+namespace {
+
+std::string tune_key(asc_graph *g, asc_algo algo) {
+    cudaDeviceProp prop;
+    std::string name = "gpu";
+    if (cudaGetDeviceProperties(&prop, g->device) == cudaSuccess) name = prop.name;
+    for (auto &c : name)
+        if (c == ' ') c = '_';
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s:V%llu:E%llu:S%llu:W%u:C%u:A%d", name.c_str(), (unsigned long long)g->V,
+             (unsigned long long)g->E, (unsigned long long)g->static_edges, g->edge_words, g->is_csc ? 1 : 0,
+             (int)algo);
+    return buf;
+}
+
+std::string tune_cache_path() {
+    const char *p = getenv("ASC_TUNE_CACHE");
+    if (p && *p) return p;
+    const char *home = getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/ascetic_gb300_tune.txt";
+}
+
+bool tune_cache_lookup(const std::string &key, asc::Tuning *t) {
+    FILE *f = fopen(tune_cache_path().c_str(), "r");
+    if (!f) return false;
+    char k[256];
+    unsigned h, sg, d, c;
+    double ms;
+    bool found = false;
+    while (fscanf(f, "%255s %u %u %u %u %lf", k, &h, &sg, &d, &c, &ms) == 6)
+        if (key == k) {
+            t->huge_degree = h;
+            t->segment_edges = sg;
+            t->dense_div = d;
+            t->ctas_per_sm = c;
+            found = true;
+        }
+    fclose(f);
+    return found;
+}
+
+void tune_cache_store(const std::string &key, const asc::Tuning &t, double ms) {
+    std::string path = tune_cache_path();
+    std::string dir = path.substr(0, path.find_last_of('/'));
+    if (!dir.empty()) {
+        std::string cmd = dir;  // create the cache directory when missing
+        mkdir(cmd.c_str(), 0755);
+    }
+    FILE *f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s %u %u %u %u %.4f\n", key.c_str(), t.huge_degree, t.segment_edges, t.dense_div, t.ctas_per_sm, ms);
+    fclose(f);
+}
+
+}  // namespace
+
+namespace asc {
+
+asc_status set_tuning(asc_graph *g, const Tuning &t) {
+    if (t.huge_degree < 32 || t.huge_degree > (1u << 20) || t.segment_edges < 256 || t.segment_edges > (1u << 24))
+        return fail(ASC_ERR_INVALID, "tuning out of range (huge %u, segment %u)", t.huge_degree, t.segment_edges);
+    free_workspace(g);  // segment capacities depend on the thresholds
+    g->tuning = t;
+    g->has_tuning = true;
+    return ASC_OK;
+}
+
+}  // namespace asc
+
+extern "C" {
+
+asc_status asc_graph_get_tuning(const asc_graph *g, asc_tuning *t) {
+    if (!g || !t) return asc::fail(ASC_ERR_INVALID, "asc_graph_get_tuning: null argument");
+    asc::Tuning d;
+    if (g->ws) d = g->ws->tune;
+    else if (g->has_tuning) d = g->tuning;
+    memset(t, 0, sizeof(*t));
+    t->huge_degree = d.huge_degree;
+    t->segment_edges = d.segment_edges;
+    t->dense_div = d.dense_div;
+    t->ctas_per_sm = d.ctas_per_sm;
+    return ASC_OK;
+}
+
+asc_status asc_graph_set_tuning(asc_graph *g, const asc_tuning *t) {
+    if (!g || !t) return asc::fail(ASC_ERR_INVALID, "asc_graph_set_tuning: null argument");
+    asc::Tuning x;
+    x.huge_degree = t->huge_degree;
+    x.segment_edges = t->segment_edges;
+    x.dense_div = t->dense_div;
+    x.ctas_per_sm = t->ctas_per_sm;
+    return asc::set_tuning(g, x);
+}
+
+asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, uint32_t flags,
+                          asc_tuning *best) {
+    using namespace asc;
+    if (!g || (!sources && algo != ASC_CC && algo != ASC_PR) || (n == 0 && algo != ASC_CC && algo != ASC_PR))
+        return fail(ASC_ERR_INVALID, "asc_graph_tune: graph and sources are required");
+    if (algo == ASC_PR) return fail(ASC_ERR_UNSUPPORTED, "tuning runs traversals (BFS, SSSP, CC)");
+    const std::string key = tune_key(g, algo);
+    Tuning cur;
+    if (g->ws) cur = g->ws->tune;
+    else if (g->has_tuning) cur = g->tuning;
+    if (!(flags & ASC_TUNE_NO_CACHE) && tune_cache_lookup(key, &cur)) {
+        ASC_TRY(set_tuning(g, cur));
+        if (best) ASC_TRY(asc_graph_get_tuning(g, best));
+        if (best) best->ms = -1;  // from the cache
+        return ASC_OK;
+    }
+    asc_params p;
+    asc_params_default(&p);
+    p.flags = ASC_RUN_NO_OUTPUT;
+    const uint32_t runs = std::max<uint32_t>(1, std::min<uint32_t>(n, 4));
+    auto measure = [&](const Tuning &t, double *ms) -> asc_status {
+        ASC_TRY(set_tuning(g, t));
+        double bestms = 1e30;
+        for (int pass = 0; pass < 2; pass++) {  // first pass warms up (graph build, caches)
+            double sum = 0;
+            for (uint32_t i = 0; i < runs; i++) {
+                asc_stats st;
+                ASC_TRY(run_traversal(g, algo, algo == ASC_CC ? 0 : sources[i], p, nullptr, &st));
+                sum += st.ms_total;
+            }
+            bestms = std::min(bestms, sum);
+        }
+        *ms = bestms;
+        return ASC_OK;
+    };
+    double cur_ms;
+    ASC_TRY(measure(cur, &cur_ms));
+    const uint32_t huge_c[] = {128, 256, 512, 1024, 4096};
+    const uint32_t seg_c[] = {1024, 2048, 4096, 8192};
+    const uint32_t div_c[] = {8, 16, 32, 64, 256, 0};
+    for (int round = 0; round < 2; round++) {
+        for (uint32_t d : div_c) {
+            Tuning t = cur;
+            t.dense_div = d;
+            if (t.dense_div == cur.dense_div) continue;
+            double ms;
+            ASC_TRY(measure(t, &ms));
+            if (ms < cur_ms) { cur = t; cur_ms = ms; }
+        }
+        for (uint32_t h : huge_c) {
+            Tuning t = cur;
+            t.huge_degree = h;
+            if (t.huge_degree == cur.huge_degree) continue;
+            double ms;
+            ASC_TRY(measure(t, &ms));
+            if (ms < cur_ms) { cur = t; cur_ms = ms; }
+        }
+        for (uint32_t sg : seg_c) {
+            Tuning t = cur;
+            t.segment_edges = sg;
+            if (t.segment_edges == cur.segment_edges) continue;
+            double ms;
+            ASC_TRY(measure(t, &ms));
+            if (ms < cur_ms) { cur = t; cur_ms = ms; }
+        }
+    }
+    ASC_TRY(set_tuning(g, cur));
+    if (!(flags & ASC_TUNE_NO_CACHE)) tune_cache_store(key, cur, cur_ms / runs);
+    if (best) {
+        ASC_TRY(asc_graph_get_tuning(g, best));
+        best->ms = cur_ms / runs;
+    }
+    return ASC_OK;
+}
+
+}  // extern "C"

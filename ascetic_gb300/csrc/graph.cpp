@@ -475,8 +475,6 @@ void asc_budget_default(asc_budget *b) {
 asc_status asc_graph_open(const char *path, asc_format fmt, const asc_budget *budget, asc_graph **out) {
     if (!path || !out) return fail(ASC_ERR_INVALID, "asc_graph_open: path and out are required");
     *out = nullptr;
-    int dev;
-    ASC_TRY(ensure_device(&dev));
     FILE *f = fopen(path, "rb");
     if (!f) return fail(ASC_ERR_BAD_FILE, "%s: cannot open (%s)", path, strerror(errno));
     struct stat sb;
@@ -532,6 +530,13 @@ asc_status asc_graph_open(const char *path, asc_format fmt, const asc_budget *bu
                     (unsigned long long)size, fmt == ASC_FMT_BCSR ? "bcsr" : fmt == ASC_FMT_BWCSR ? "bwcsr"
                                               : fmt == ASC_FMT_BCSC ? "bcsc" : "bcsr32",
                     (unsigned long long)V, (unsigned long long)E, (unsigned long long)expect);
+    }
+    // the file's layout and size check out: now the device is needed
+    int dev;
+    s = ensure_device(&dev);
+    if (s != ASC_OK) {
+        fclose(f);
+        return s;
     }
     asc_graph *g = new asc_graph();
     g->V = V;

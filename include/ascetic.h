@@ -191,6 +191,27 @@ asc_status asc_sssp_opt(const char *path, uint32_t source, double advise_rate, u
                         asc_stats *stats);
 asc_status asc_pr_opt(const char *path, double advise_rate, double *out, asc_stats *stats);
 
+/* ---- tuning ------------------------------------------------------------------- */
+/* The engine's tunables for one graph: lists longer than huge_degree edges are
+ * cut into segment_edges-edge work items; a region whose frontier holds more
+ * than 1/dense_div of its vertices is walked in id order through the frontier
+ * bitmap (0: never); ctas_per_sm sizes the persistent grids (0: as many as stay
+ * resident). ms is the measured time per run of the chosen setting (-1 when
+ * it came from the cache). No reference counterpart (its launch shape is fixed
+ * at 56 x 1024, GraphMeta.cuh:55-56). */
+typedef struct asc_tuning {
+    uint32_t huge_degree, segment_edges, dense_div, ctas_per_sm;
+    double ms;
+} asc_tuning;
+enum { ASC_TUNE_NO_CACHE = 1u << 0 };
+asc_status asc_graph_get_tuning(const asc_graph *g, asc_tuning *t);
+asc_status asc_graph_set_tuning(asc_graph *g, const asc_tuning *t);
+/* Measures candidate settings on runs of algo (BFS/SSSP from the given
+ * sources, CC from all vertices) and keeps the fastest for the graph's later
+ * runs. Cached per GPU and graph shape unless ASC_TUNE_NO_CACHE. */
+asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n, uint32_t flags,
+                          asc_tuning *best);
+
 /* ---- query server ----------------------------------------------------------- */
 /* Serves BFS / SSSP / CC / PageRank queries against several resident graphs on
  * one GPU under one device-memory budget. In ASC_SERVE_BATCHED mode BFS and

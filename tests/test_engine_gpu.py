@@ -170,6 +170,34 @@ def test_pagerank_scatter_on_out_edge_graphs(weighted):
             assert np.abs(got.astype(np.float64) - exp).max() <= PR_TOL, prec
 
 
+@pytest.mark.parametrize("huge,seg,div", [(32, 256, 1), (64, 4096, 0), (4096, 1024, 16), (512, 2048, 2)])
+def test_tunables_do_not_change_results(huge, seg, div):
+    ptr, adj = A.rmat_csr(13, 16, 34, weights=(1, 63))
+    col = adj[:, 0].copy()
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=0.3)) as g:
+        g.set_tuning(huge_degree=huge, segment_edges=seg, dense_div=div)
+        assert g.get_tuning()["huge_degree"] == huge
+        for s in (0, 99):
+            got, _ = g.run("bfs", s)
+            assert np.array_equal(got, oracle.bfs(ptr, col, s))
+            got, _ = g.run("sssp", s)
+            assert np.array_equal(got, oracle.sssp(ptr, adj, s))
+        got, _ = g.run_batch("bfs", [0, 99, 5])
+        assert np.array_equal(got[1], oracle.bfs(ptr, col, 99))
+
+
+def test_autotuner_picks_a_working_setting(tmp_path, monkeypatch):
+    monkeypatch.setenv("ASC_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    ptr, col = A.rmat_csr(14, 16, 35)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.25)) as g:
+        best = g.tune("bfs", [0, 5])
+        assert best["ms"] > 0 and best["huge_degree"] >= 32
+        got, _ = g.run("bfs", 5)
+        assert np.array_equal(got, oracle.bfs(ptr, col, 5))
+        again = g.tune("bfs", [0, 5])          # served from the cache
+        assert again["ms"] == -1 and again["huge_degree"] == best["huge_degree"]
+
+
 def test_huge_vertices_and_segments():
     """A star whose hub list is far above the segment threshold, mostly on demand."""
     V = 50000

@@ -105,3 +105,31 @@ def test_invalid_generator_arguments():
 def test_ptgraph_cli_prints_usage():
     r = subprocess.run([A.PTGRAPH_PATH], capture_output=True, text=True)
     assert r.returncode == 1 and "usage: ptgraph" in r.stderr
+
+
+def _write_small(path, fmt):
+    p, e = A.rmat_csr(8, 4, 9)
+    A.write_graph(path, fmt, p, e)
+    return p, e
+
+
+def test_malformed_files_are_rejected_before_any_device_work():
+    """A short file, a header that matches no layout, and an ambiguous size all
+    return ASC_ERR_BAD_FILE (checked on the host, no GPU needed)."""
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "g.bcsr")
+    _write_small(path, A.FMT_BCSR)
+    raw = open(path, "rb").read()
+    for name, data in [("short.bcsr", raw[:-40]), ("tiny.bcsr", raw[:6]), ("junk.bcsr", b"\xff" * 64)]:
+        bad = os.path.join(d, name)
+        open(bad, "wb").write(data)
+        with pytest.raises(A.AscError) as e:
+            A.Graph.open(bad)
+        assert e.value.status == A.ERR_BAD_FILE, name
+    # explicit layout that does not match the size
+    with pytest.raises(A.AscError) as e:
+        A.Graph.open(path, fmt=A.FMT_BWCSR)
+    assert e.value.status == A.ERR_BAD_FILE
+    with pytest.raises(A.AscError) as e:
+        A.Graph.open(os.path.join(d, "missing.bcsr"))
+    assert e.value.status == A.ERR_BAD_FILE
