@@ -58,6 +58,10 @@ def parse():
                          "20,22,24,26 is the full serving configuration")
     ap.add_argument("--serve-queries", type=int, default=400)
     ap.add_argument("--serve-budget-gb", type=float, default=12.0)
+    ap.add_argument("--pr-study", type=int, default=0,
+                    help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
+                         "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
+    ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
     return ap.parse_args()
 
 
@@ -165,6 +169,40 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def pr_study(args):
+    """PageRank precision study: standard PageRank (damping 0.85, uniform start,
+    dangling mass spread uniformly, stop at FP64 L1 residual < 1e-9 or 100
+    passes) on the in-edge (CSC) arrays of an RMAT graph, FP32 ranks/sums with
+    FP64 residual and dangling reductions vs an all-FP64 GPU run vs the FP64
+    host oracle; max-abs and L1 error of each."""
+    import ascetic_gb300 as A
+    import oracle
+    t0 = time.time()
+    cptr, ccol, od = A.rmat_csr(args.pr_study, 16, 3, transpose=True)
+    gen_s = time.time() - t0
+    out = {"study": "pagerank precision", "rmat_scale": args.pr_study, "edges": int(cptr[-1]),
+           "budget_frac": 0.30, "generate_s": round(gen_s, 1)}
+    with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=0.30)) as g:
+        res = {}
+        for name, prec in (("fp32", A.F32), ("fp64", A.F64)):
+            prm = A.make_params(pr_mode=A.PR_STD, precision=prec)
+            g.run("pr", params=prm)
+            r, st = g.run("pr", params=prm)
+            res[name] = (r.astype(np.float64), st)
+    t1 = time.perf_counter()
+    exact, it, resid = oracle.pr_std(cptr, ccol, od)
+    oracle_s = time.perf_counter() - t1
+    for name, (r, st) in res.items():
+        out[name] = {"ms": round(st["ms_total"], 2), "passes": st["iterations"], "residual": st["residual"],
+                     "max_abs_err_vs_fp64_oracle": float(np.abs(r - exact).max()),
+                     "l1_err_vs_fp64_oracle": float(np.abs(r - exact).sum()),
+                     "ondemand_bytes": st["ondemand_bytes"]}
+    out["fp32_vs_fp64_gpu_max_abs"] = float(np.abs(res["fp32"][0] - res["fp64"][0]).max())
+    out["oracle"] = {"passes": it, "residual": resid, "seconds_1_core": round(oracle_s, 1)}
+    out["within_1e-6"] = bool(out["fp32"]["max_abs_err_vs_fp64_oracle"] <= 1e-6)
+    print(json.dumps(out), flush=True)
+
+
 def serve_leg(args):
     """Serving: BFS/SSSP/CC/PR queries (mix 50/30/10/10, graph uniform, sources
     uniform over vertices with out-degree > 0) against resident RMAT graphs
@@ -264,6 +302,9 @@ def workload_config(args):
 
 def main():
     args = parse()
+    if args.pr_study:
+        pr_study(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return
@@ -381,6 +422,24 @@ def main():
                              "ondemand_bytes": bst["ondemand_bytes"], "iterations": bst["iterations"],
                              "rows_checked_bit_exact": 4, "bit_exact": bool(exact)}
     g.close()
+    if args.batch and args.batch_sssp:
+        _, adjb = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
+        with A.Graph.from_csr(ptr, adjb, budget=budget) as gw:
+            bsrc = pick_sources(ptr, args.batch, args.seed + 200)
+            gw.run_batch("sssp", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+            _, bst = gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+            seq_ms = 0.0
+            for s_ in bsrc:
+                _, st = gw.run("sssp", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+                seq_ms += st["ms_total"]
+            rows, _ = gw.run_batch("sssp", bsrc[:4])
+            exact = all(np.array_equal(rows[i], gw.run("sssp", s_)[0]) for i, s_ in enumerate(bsrc[:4]))
+            line["batch_sssp"] = {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
+                                  "sequential_ms": round(seq_ms, 3),
+                                  "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
+                                  "iterations": bst["iterations"], "rows_checked_bit_exact": 4,
+                                  "bit_exact": bool(exact)}
+        del adjb
 
     if not args.quick:
         extra = {}
