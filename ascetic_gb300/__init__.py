@@ -71,10 +71,11 @@ class GraphInfo(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("huge_degree", ctypes.c_uint32), ("segment_edges", ctypes.c_uint32),
-                ("dense_div", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32), ("ms", ctypes.c_double)]
+                ("dense_div", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32), ("delta", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("ms", ctypes.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class ServerConfig(ctypes.Structure):
@@ -344,8 +345,8 @@ def _get_tuning(self):
     return t.as_dict()
 
 
-def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0):
-    t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, 0.0)
+def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=64):
+    t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, delta, 0, 0.0)
     _check(lib().asc_graph_set_tuning(self._h, ctypes.byref(t)))
 
 

@@ -32,8 +32,10 @@ def _nvcc():
 
 
 def _common_flags():
+    # ASC_NVCC_EXTRA: extra nvcc flags (e.g. -DASC_EXPAND_MIN_BLOCKS=6) for tuning experiments
+    extra = os.environ.get("ASC_NVCC_EXTRA", "").split()
     return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
-            "-I" + INCLUDE, "-I" + CSRC]
+            "-I" + INCLUDE, "-I" + CSRC] + extra
 
 
 def _stale(target, deps):

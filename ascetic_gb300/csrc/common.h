@@ -39,6 +39,8 @@ struct Tuning {
     uint32_t ctas_per_sm = 4;     // persistent expansion grid = SMs x this
     uint32_t dense_div = 64;      // walk a region in id order (frontier bitmap) when its list
                                   // holds more than 1/dense_div of the region's vertices; 0 = never
+    uint32_t delta = 64;          // SSSP near-far step: distances >= threshold wait in the far set,
+                                  // the threshold advances to (min far distance + delta); 0 = off
 };
 
 // Per-run device state, sized for one graph and reused across its runs.
@@ -48,6 +50,7 @@ struct Workspace {
     uint32_t *bitmap[2] = {nullptr, nullptr};  // frontier membership by parity, one bit per vertex
     uint32_t *visited = nullptr;     // BFS: one bit per vertex already reached
     uint32_t *huge_bits = nullptr;   // one bit per vertex with more than huge_degree edges
+    uint32_t *far_bits = nullptr;    // SSSP: vertices waiting for the threshold to reach them
     uint32_t *queue[2] = {nullptr, nullptr};   // [V]: static entries from 0, on-demand from S
     uint64_t *segs[2] = {nullptr, nullptr};    // segment items (v << 32 | k)
     uint64_t segcap_static = 0, segcap_ondemand = 0;

@@ -43,6 +43,10 @@ namespace asc {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+// Minimum resident CTAs per SM asked of the expansion kernels (register cap).
+#ifndef ASC_EXPAND_MIN_BLOCKS
+#define ASC_EXPAND_MIN_BLOCKS 4
+#endif
 constexpr int kWarps = kBlock / 32;
 
 enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
@@ -55,9 +59,10 @@ enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 // static, frontier vertices on-demand, reached vertices, reached edges. PageRank FP64 accumulators at word 32:
 // residual[2], dangling[2].
 // Word 28 counts iterations, word 29 flags an iteration cap hit and word 30
-// counts loop-body executions when the loop runs as a CUDA graph.
-enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_ITERS = 28, CTL_TIMEOUT = 29, CTL_BODIES = 30, CTL_PR = 32,
-       CTL_WORDS = 64 };
+// counts loop-body executions when the loop runs as a CUDA graph. Word 31 is
+// the SSSP near-far threshold, word 36 the minimum far distance of a pass.
+enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_ITERS = 28, CTL_TIMEOUT = 29, CTL_BODIES = 30, CTL_THRESH = 31,
+       CTL_PR = 32, CTL_MINFAR = 36, CTL_WORDS = 64 };
 
 struct RegionArgs {
     const uint32_t *ptr;
@@ -66,6 +71,8 @@ struct RegionArgs {
     uint32_t *bitmap;             // next-frontier bitmap (written)
     uint32_t *visited;            // BFS: reached-vertex bitmap (claims)
     const uint32_t *huge_bits;    // one bit per vertex whose list is cut into segments
+    uint32_t *far_bits;           // SSSP near-far: vertices whose distance is at or above *thresh
+    const uint32_t *thresh;
     const uint32_t *bitmap_in;    // this iteration's frontier bitmap (null: no id-order mode)
     const uint32_t *q_in;         // this region's input list (null: dense range)
     const uint64_t *seg_in;       // this region's input segments
@@ -214,6 +221,10 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
     if (nv >= cur) return false;
     uint32_t old = atomicMin(&a.val[v], nv);
     if (nv >= old) return false;
+    if (ALG == kSSSP && a.far_bits && nv >= *a.thresh) {
+        atomicOr(&a.far_bits[v >> 5], bit);  // waits until the threshold reaches it
+        return false;
+    }
     return (atomicOr(&a.bitmap[v >> 5], bit) & bit) == 0;
 }
 
@@ -254,8 +265,9 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
     sm.vu[threadIdx.x] = vu;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(act);
-    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
-        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+    // software pipeline: the column loads of the next pass are in flight while
+    // this pass probes and updates its destinations
+    auto load_pass = [&](uint32_t base, uint32_t (&v)[kUnroll], uint32_t (&nv)[kUnroll]) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t e = base + k * kBlock + threadIdx.x;
@@ -271,10 +283,21 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
                 load_edge<ALG, WORDS>(a, sm.vu[lo], (uint64_t)sm.start[lo] + (e - sm.pref[lo]), v[k], nv[k]);
             }
         }
+    };
+    uint32_t v[kUnroll], nv[kUnroll];
+    if (total) load_pass(0, v, nv);
+    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
+        uint32_t vn[kUnroll], nvn[kUnroll], cur[kUnroll];
+        if (base + kUnroll * kBlock < total) load_pass(base + kUnroll * kBlock, vn, nvn);
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            v[k] = vn[k];
+            nv[k] = nvn[k];
+        }
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -291,8 +314,7 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     const uint32_t vu = a.val[u];
-    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
-        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+    auto load_pass = [&](uint32_t base, uint32_t (&v)[kUnroll], uint32_t (&nv)[kUnroll]) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
@@ -300,10 +322,21 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
             nv[k] = 0xffffffffu;
             if (j < n) load_edge<ALG, WORDS>(a, vu, b + j, v[k], nv[k]);
         }
+    };
+    uint32_t v[kUnroll], nv[kUnroll];
+    if (n) load_pass(0, v, nv);
+    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
+        uint32_t vn[kUnroll], nvn[kUnroll], cur[kUnroll];
+        if (base + kUnroll * kBlock < n) load_pass(base + kUnroll * kBlock, vn, nvn);
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            v[k] = vn[k];
+            nv[k] = nvn[k];
+        }
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
@@ -351,7 +384,7 @@ __device__ __forceinline__ void flush_next(const RegionArgs &a, uint32_t *s_next
 }
 
 template <int ALG, int WORDS>
-__global__ void __launch_bounds__(kBlock) expand_kernel(RegionArgs a) {
+__global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_kernel(RegionArgs a) {
     __shared__ Smem sm;
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
@@ -380,7 +413,7 @@ struct FusedArgs {
 };
 
 template <int ALG, int WORDS>
-__global__ void __launch_bounds__(kBlock) expand_fused_kernel(FusedArgs x) {
+__global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_kernel(FusedArgs x) {
     __shared__ Smem sm;
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
@@ -483,6 +516,62 @@ __global__ void build_frontier_kernel(RegionArgs a, const uint32_t *next_bits, u
             x &= x - 1;
             a.q_out[a.S + b1++] = v0 + b;
         }
+    }
+}
+
+// SSSP near-far, step 1: when the pass left the near frontier empty, the
+// smallest distance in the far set (atomicMin into the control block).
+__global__ void far_min_kernel(RegionArgs a, uint32_t nwords, uint32_t *minfar) {
+    if (a.cnt_out[6] | a.cnt_out[7]) return;
+    uint32_t m = 0xffffffffu;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        uint32_t word = a.far_bits[w];
+        while (word) {
+            const int b = __ffs(word) - 1;
+            word &= word - 1;
+            m = min(m, a.val[32 * w + b]);
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_down_sync(kFull, m, d));
+    if ((threadIdx.x & 31) == 0 && m != 0xffffffffu) atomicMin(minfar, m);
+}
+
+// SSSP near-far, step 2: the threshold moves to (min far distance + delta) and
+// every far vertex below it joins the next frontier (bit and region count).
+__global__ void far_promote_kernel(RegionArgs a, uint32_t nwords, const uint32_t *minfar, uint32_t *thresh,
+                                   uint32_t delta) {
+    if (a.cnt_out[6] | a.cnt_out[7]) return;
+    const uint32_t mf = *minfar;
+    if (mf == 0xffffffffu) return;
+    const uint32_t t = mf > 0xffffffffu - delta ? 0xffffffffu : mf + delta;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *thresh = t;
+    uint32_t n0 = 0, n1 = 0;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const uint32_t word = a.far_bits[w];
+        if (!word) continue;
+        uint32_t x = word, promo = 0;
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            if (a.val[32 * w + b] < t) promo |= 1u << b;
+        }
+        if (!promo) continue;
+        a.far_bits[w] = word & ~promo;
+        a.bitmap[w] |= promo;
+        const uint32_t v0 = 32 * w;
+        const uint32_t smask = v0 + 32 <= a.S ? 0xffffffffu : (v0 >= a.S ? 0 : (1u << (a.S - v0)) - 1u);
+        n0 += __popc(promo & smask);
+        n1 += __popc(promo & ~smask);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        n0 += __shfl_down_sync(kFull, n0, d);
+        n1 += __shfl_down_sync(kFull, n1, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (n0) atomicAdd(&a.cnt_out[6], n0);
+        if (n1) atomicAdd(&a.cnt_out[7], n1);
     }
 }
 
@@ -886,6 +975,7 @@ asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
     for (int i = 0; i < 2; i++) ASC_TRY(dalloc((void **)&ws->bitmap[i], 4 * (V / 32 + 2)));
     ASC_TRY(dalloc((void **)&ws->visited, 4 * (V / 32 + 2)));
     ASC_TRY(dalloc((void **)&ws->huge_bits, 4 * (V / 32 + 2)));
+    ASC_TRY(dalloc((void **)&ws->far_bits, 4 * (V / 32 + 2)));
     ASC_CUDA(cudaMemcpy(ws->huge_bits, hbits.data(), 4 * (V / 32 + 2), cudaMemcpyHostToDevice));
     for (int i = 0; i < 2; i++) {
         ASC_TRY(dalloc((void **)&ws->queue[i], 4 * V));
@@ -969,6 +1059,17 @@ RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
     return region_args(g, g->ws, parity_in, region, dense);
 }
 
+// SSSP near-far on: the expansion parks distances at or above the threshold in
+// the far set.
+bool near_far(asc_graph *g, asc_algo algo) { return algo == ASC_SSSP && g->ws->tune.delta != 0; }
+
+void attach_far(asc_graph *g, asc_algo algo, RegionArgs &a) {
+    if (near_far(g, algo)) {
+        a.far_bits = g->ws->far_bits;
+        a.thresh = g->ws->ctl + CTL_THRESH;
+    }
+}
+
 uint32_t grid_for(const Workspace *ws, uint64_t work_items) {
     uint64_t cap = (uint64_t)ws->num_sms * ws->tune.ctas_per_sm;
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(cap, work_items));
@@ -978,6 +1079,17 @@ uint32_t fill_grid(const Workspace *ws, uint64_t n) {
     uint64_t blocks = (n + kBlock - 1) / kBlock;
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)ws->num_sms * 8));
 }
+
+// The near-far promotion after an expansion (no-ops when the near frontier is
+// not empty or the far set is).
+void launch_far(asc_graph *g, cudaStream_t s, const RegionArgs &out_args) {
+    Workspace *ws = g->ws;
+    const uint32_t nwords = (uint32_t)g->V / 32 + 1;
+    far_min_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(out_args, nwords, ws->ctl + CTL_MINFAR);
+    far_promote_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(out_args, nwords, ws->ctl + CTL_MINFAR,
+                                                                 ws->ctl + CTL_THRESH, ws->tune.delta);
+}
+
 
 template <int ALG, int WORDS>
 void launch_expand(asc_graph *g, const RegionArgs &a, uint32_t grid) {
@@ -1083,8 +1195,12 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
                     FusedArgs x;
                     x.r0 = region_args(g, parity, 0, false);
                     x.r1 = region_args(g, parity, 1, false);
+                    attach_far(g, algo, x.r0);
+                    attach_far(g, algo, x.r1);
                     x.work = x.r0.cnt_out + 4;
+                    if (near_far(g, algo)) cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, cs);
                     fused(cs, x, grid);
+                    if (near_far(g, algo)) launch_far(g, cs, x.r0);
                     build_frontier_kernel<<<fill_grid(ws, V / 32 + 1), kBlock, 0, cs>>>(x.r0, ws->bitmap[po],
                                                                                         V / 32 + 1);
                 }
@@ -1110,7 +1226,8 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 }  // namespace
 
 void free_ws_buffers(Workspace *ws) {
-    for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->bitmap[0],
+    for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->far_bits,
+                    (void *)ws->bitmap[0],
                     (void *)ws->bitmap[1],
                     (void *)ws->queue[0],
                     (void *)ws->queue[1],
@@ -1158,6 +1275,12 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     if (algo == ASC_CC) init_values_kernel<kCC><<<ig, kBlock, 0, s>>>(ws->val, V, 0);
     else if (algo == ASC_BFS) init_values_kernel<kBFS><<<ig, kBlock, 0, s>>>(ws->val, V, source);
     else init_values_kernel<kSSSP><<<ig, kBlock, 0, s>>>(ws->val, V, source);
+    if (near_far(g, algo)) {
+        ASC_CUDA(cudaMemsetAsync(ws->far_bits, 0, 4 * (V / 32 + 2), s));
+        ASC_CUDA(cudaStreamSynchronize(s));  // the staging word below is host memory
+        ws->h_ctl[CTL_THRESH] = 1 + ws->tune.delta;
+        ASC_CUDA(cudaMemcpyAsync(ws->ctl + CTL_THRESH, ws->h_ctl + CTL_THRESH, 4, cudaMemcpyHostToDevice, s));
+    }
     // the seeded frontier lands in parity 0 (as the output of a virtual pass from parity 1)
     RegionArgs sa = base_args(g, 1);
     const uint32_t nwords = V / 32 + 1;
@@ -1197,10 +1320,12 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
         if (pt.on) {
             // diagnostic: one launch per region, each timed on its own
+            if (near_far(g, algo)) ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, s));
             for (int region = 0; region < 2; region++) {
                 const uint64_t items = region_work(region);
                 if (!items) continue;
                 RegionArgs a = region_args(g, parity, region, false);
+                attach_far(g, algo, a);
                 ASC_TRY(pt.begin(region));
                 pt.record(s);
                 expand(g, a, grid_for(ws, items));
@@ -1212,12 +1337,22 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
             FusedArgs x;
             x.r0 = region_args(g, parity, 0, false);
             x.r1 = region_args(g, parity, 1, false);
+            attach_far(g, algo, x.r0);
+            attach_far(g, algo, x.r1);
             x.work = x.r0.cnt_out + 4;
+            if (near_far(g, algo)) ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, s));
             fused(s, x, grid_for(ws, items));
             launches++;
         }
-        build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(region_args(g, parity, 0, false),
-                                                                        ws->bitmap[po], nwords);
+        {
+            RegionArgs out_args = region_args(g, parity, 0, false);
+            attach_far(g, algo, out_args);
+            if (near_far(g, algo)) {
+                launch_far(g, s, out_args);
+                launches += 2;
+            }
+            build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(out_args, ws->bitmap[po], nwords);
+        }
         launches++;
         ASC_CUDA(cudaGetLastError());
         ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
@@ -1244,7 +1379,8 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     ASC_CUDA(cudaStreamSynchronize(s));
     if (use_graph) {
         iters = (int)ws->h_ctl[CTL_ITERS];
-        launches += 5 * ws->h_ctl[CTL_BODIES] - 1;  // two expansions, two builds and the loop test per body
+        // per body: two expansions, two builds (and two near-far pairs), the loop test
+        launches += (near_far(g, algo) ? 9 : 5) * ws->h_ctl[CTL_BODIES] - 1;
         if (ws->h_ctl[CTL_TIMEOUT]) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
     }
     if (st) {
@@ -2698,15 +2834,16 @@ bool tune_cache_lookup(const std::string &key, asc::Tuning *t) {
     FILE *f = fopen(tune_cache_path().c_str(), "r");
     if (!f) return false;
     char k[256];
-    unsigned h, sg, d, c;
+    unsigned h, sg, d, c, dl;
     double ms;
     bool found = false;
-    while (fscanf(f, "%255s %u %u %u %u %lf", k, &h, &sg, &d, &c, &ms) == 6)
+    while (fscanf(f, "%255s %u %u %u %u %u %lf", k, &h, &sg, &d, &c, &dl, &ms) == 7)
         if (key == k) {
             t->huge_degree = h;
             t->segment_edges = sg;
             t->dense_div = d;
             t->ctas_per_sm = c;
+            t->delta = dl;
             found = true;
         }
     fclose(f);
@@ -2722,7 +2859,8 @@ void tune_cache_store(const std::string &key, const asc::Tuning &t, double ms) {
     }
     FILE *f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%s %u %u %u %u %.4f\n", key.c_str(), t.huge_degree, t.segment_edges, t.dense_div, t.ctas_per_sm, ms);
+    fprintf(f, "%s %u %u %u %u %u %.4f\n", key.c_str(), t.huge_degree, t.segment_edges, t.dense_div, t.ctas_per_sm,
+            t.delta, ms);
     fclose(f);
 }
 
@@ -2753,6 +2891,7 @@ asc_status asc_graph_get_tuning(const asc_graph *g, asc_tuning *t) {
     t->segment_edges = d.segment_edges;
     t->dense_div = d.dense_div;
     t->ctas_per_sm = d.ctas_per_sm;
+    t->delta = d.delta;
     return ASC_OK;
 }
 
@@ -2763,6 +2902,7 @@ asc_status asc_graph_set_tuning(asc_graph *g, const asc_tuning *t) {
     x.segment_edges = t->segment_edges;
     x.dense_div = t->dense_div;
     x.ctas_per_sm = t->ctas_per_sm;
+    x.delta = t->delta;
     return asc::set_tuning(g, x);
 }
 
@@ -2806,7 +2946,17 @@ asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, 
     const uint32_t huge_c[] = {128, 256, 512, 1024, 4096};
     const uint32_t seg_c[] = {1024, 2048, 4096, 8192};
     const uint32_t div_c[] = {8, 16, 32, 64, 256, 0};
+    const uint32_t delta_c[] = {0, 16, 32, 64, 128, 256};
     for (int round = 0; round < 2; round++) {
+        if (algo == ASC_SSSP)
+            for (uint32_t dl : delta_c) {
+                Tuning t = cur;
+                t.delta = dl;
+                if (t.delta == cur.delta) continue;
+                double ms;
+                ASC_TRY(measure(t, &ms));
+                if (ms < cur_ms) { cur = t; cur_ms = ms; }
+            }
         for (uint32_t d : div_c) {
             Tuning t = cur;
             t.dense_div = d;

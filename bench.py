@@ -446,13 +446,18 @@ def main():
         _, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
         with A.Graph.from_csr(ptr, adj, budget=budget) as gw:
             gw.run("sssp", srcs[0], params=A.make_params(flags=A.RUN_NO_OUTPUT))
-            e, ms = 0, 0.0
+            e, ms, proc, its = 0, 0.0, 0, 0
             for s in srcs[:4]:
                 _, st = gw.run("sssp", s, params=A.make_params(flags=A.RUN_NO_OUTPUT))
                 e += st["reached_edges"]
                 ms += st["ms_total"]
+                proc += st["edges_processed"]
+                its += st["iterations"]
             extra["sssp_gteps"] = round(e / (ms * 1e-3) / 1e9, 4)
             extra["sssp_ms"] = round(ms / 4, 3)
+            extra["sssp_processed_per_reached_edge"] = round(proc / e, 3) if e else None
+            extra["sssp_iterations"] = its / 4
+            extra["sssp_tuning"] = gw.get_tuning()
         del adj
         sp, sc = A.rmat_csr(args.scale, args.edge_factor, args.seed, symmetric=True)
         with A.Graph.from_csr(sp, sc, budget=budget) as gs:

@@ -196,11 +196,15 @@ asc_status asc_pr_opt(const char *path, double advise_rate, double *out, asc_sta
  * cut into segment_edges-edge work items; a region whose frontier holds more
  * than 1/dense_div of its vertices is walked in id order through the frontier
  * bitmap (0: never); ctas_per_sm sizes the persistent grids (0: as many as stay
- * resident). ms is the measured time per run of the chosen setting (-1 when
+ * resident); delta is the SSSP near-far step. ms is the measured time per run of the chosen setting (-1 when
  * it came from the cache). No reference counterpart (its launch shape is fixed
  * at 56 x 1024, GraphMeta.cuh:55-56). */
 typedef struct asc_tuning {
     uint32_t huge_degree, segment_edges, dense_div, ctas_per_sm;
+    uint32_t delta;  /* SSSP near-far step: relaxed distances at or above the threshold wait in a far
+                        set; when the near frontier empties the threshold moves to the smallest far
+                        distance + delta (0: plain frontier relaxation) */
+    uint32_t reserved;
     double ms;
 } asc_tuning;
 enum { ASC_TUNE_NO_CACHE = 1u << 0 };

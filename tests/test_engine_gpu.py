@@ -170,12 +170,13 @@ def test_pagerank_scatter_on_out_edge_graphs(weighted):
             assert np.abs(got.astype(np.float64) - exp).max() <= PR_TOL, prec
 
 
-@pytest.mark.parametrize("huge,seg,div", [(32, 256, 1), (64, 4096, 0), (4096, 1024, 16), (512, 2048, 2)])
-def test_tunables_do_not_change_results(huge, seg, div):
+@pytest.mark.parametrize("huge,seg,div,delta", [(32, 256, 1, 1), (64, 4096, 0, 0), (4096, 1024, 16, 64),
+                                                (512, 2048, 2, 1000)])
+def test_tunables_do_not_change_results(huge, seg, div, delta):
     ptr, adj = A.rmat_csr(13, 16, 34, weights=(1, 63))
     col = adj[:, 0].copy()
     with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=0.3)) as g:
-        g.set_tuning(huge_degree=huge, segment_edges=seg, dense_div=div)
+        g.set_tuning(huge_degree=huge, segment_edges=seg, dense_div=div, delta=delta)
         assert g.get_tuning()["huge_degree"] == huge
         for s in (0, 99):
             got, _ = g.run("bfs", s)
