@@ -66,7 +66,8 @@ class GraphInfo(ctypes.Structure):
                 ("is_csc", ctypes.c_uint32), ("static_edges", ctypes.c_uint64),
                 ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
-                ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32)]
+                ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32),
+                ("weight_bits", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class Tuning(ctypes.Structure):
@@ -345,7 +346,7 @@ def _get_tuning(self):
     return t.as_dict()
 
 
-def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=64):
+def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=0):
     t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, delta, 0, 0.0)
     _check(lib().asc_graph_set_tuning(self._h, ctypes.byref(t)))
 

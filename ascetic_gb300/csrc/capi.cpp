@@ -42,7 +42,7 @@ static asc_status check_algo(asc_graph *g, asc_algo algo, uint32_t source) {
         case ASC_BFS:
         case ASC_SSSP:
             if (g->is_csc) return fail(ASC_ERR_UNSUPPORTED, "BFS/SSSP read out-edges; this graph holds in-edges (bcsc)");
-            if (algo == ASC_SSSP && g->edge_words != 2)
+            if (algo == ASC_SSSP && g->edge_words != 2 && g->wbits == 0)
                 return fail(ASC_ERR_UNSUPPORTED, "SSSP needs a weighted graph ({dst, weight} edges, bwcsr)");
             if (source >= g->V)
                 return fail(ASC_ERR_INVALID, "source %u is not a vertex (V = %llu)", source, (unsigned long long)g->V);

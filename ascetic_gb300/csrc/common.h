@@ -39,7 +39,7 @@ struct Tuning {
     uint32_t ctas_per_sm = 4;     // persistent expansion grid = SMs x this
     uint32_t dense_div = 64;      // walk a region in id order (frontier bitmap) when its list
                                   // holds more than 1/dense_div of the region's vertices; 0 = never
-    uint32_t delta = 64;          // SSSP near-far step: distances >= threshold wait in the far set,
+    uint32_t delta = 0;           // SSSP near-far step: distances >= threshold wait in the far set,
                                   // the threshold advances to (min far distance + delta); 0 = off
 };
 
@@ -77,7 +77,9 @@ struct Workspace {
 
 struct asc_graph {
     uint64_t V = 0, E = 0;
-    uint32_t edge_words = 1;      // 1: u32 destination, 2: {dst, weight}
+    uint32_t edge_words = 1;      // 1: u32 destination (or packed dst/weight), 2: {dst, weight}
+    uint32_t wbits = 0;           // > 0: weighted edges packed as (dst << wbits) | weight in one u32
+    uint32_t file_edge_bytes = 4; // bytes per edge of the source layout (the budget's unit)
     bool is_csc = false;
     uint32_t max_degree = 0;
     uint32_t max_weight = 0;

@@ -90,6 +90,7 @@ struct RegionArgs {
     uint32_t segcap_static;
     uint32_t V;
     uint32_t dense_div;
+    uint32_t wbits;               // > 0: u32 edges packed as (dst << wbits) | weight
 };
 
 // How a tile picks its vertices: from the frontier list, every vertex of a
@@ -178,14 +179,12 @@ __device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint
         v = e.x;
         nv = ALG == kSSSP ? vu + e.y : (ALG == kBFS ? vu + 1 : vu);
     } else {
-        v = __ldg(a.edges + idx);
-        nv = ALG == kBFS ? vu + 1 : vu;
+        const uint32_t e = __ldg(a.edges + idx);
+        v = e >> a.wbits;
+        nv = ALG == kBFS ? vu + 1 : (ALG == kSSSP ? vu + (e & ((1u << a.wbits) - 1u)) : vu);
     }
 }
 
-// What a thread reads about v before deciding to update it: BFS reads the
-// word of the reached-vertex bitmap (V/8 bytes, cache resident), the others
-// the value itself.
 // Counts, per region, the vertices whose next-frontier bit this warp won
 // (shared-memory counters, flushed once per CTA). Every lane calls it.
 __device__ __forceinline__ void count_next(const RegionArgs &a, bool won, uint32_t v, uint32_t *s_next) {
@@ -1023,6 +1022,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.visited = ws->visited;
     a.huge_bits = ws->huge_bits;
     a.dense_div = ws->tune.dense_div;
+    a.wbits = g->wbits;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
     a.huge = ws->tune.huge_degree;
@@ -1107,13 +1107,13 @@ void launch_fused(cudaStream_t s, const FusedArgs &x, uint32_t grid) {
 FusedFn pick_fused(asc_algo algo, uint32_t words) {
     if (algo == ASC_BFS) return words == 2 ? launch_fused<kBFS, 2> : launch_fused<kBFS, 1>;
     if (algo == ASC_CC) return words == 2 ? launch_fused<kCC, 2> : launch_fused<kCC, 1>;
-    return launch_fused<kSSSP, 2>;
+    return words == 2 ? launch_fused<kSSSP, 2> : launch_fused<kSSSP, 1>;
 }
 
 ExpandFn pick_expand(asc_algo algo, uint32_t words) {
     if (algo == ASC_BFS) return words == 2 ? launch_expand<kBFS, 2> : launch_expand<kBFS, 1>;
     if (algo == ASC_CC) return words == 2 ? launch_expand<kCC, 2> : launch_expand<kCC, 1>;
-    return launch_expand<kSSSP, 2>;
+    return words == 2 ? launch_expand<kSSSP, 2> : launch_expand<kSSSP, 1>;
 }
 
 // Per-iteration phase timing with events on the engine's stream.
@@ -1660,7 +1660,7 @@ __device__ void ms_tile(const MsArgs &m, const RegionArgs &a, uint32_t tile, uin
                     else hi = mid;
                 }
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
-                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx);
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx) >> a.wbits;
                 fk[k] = sm.f[lo];
             }
         }
@@ -1692,7 +1692,7 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
             ok[k] = j < n;
-            v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j)) : 0;
+            v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j) >> a.wbits) : 0;
         }
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
@@ -1753,9 +1753,15 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
     for (uint32_t c = 0; c < n; c += 32) {
         uint32_t ev = 0, ew = 0;
         if (c + lane < n) {
-            const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
-            ev = e.x;
-            ew = e.y;
+            if (a.wbits) {
+                const uint32_t e = __ldg(a.edges + b + c + lane);
+                ev = e >> a.wbits;
+                ew = e & ((1u << a.wbits) - 1u);
+            } else {
+                const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
+                ev = e.x;
+                ew = e.y;
+            }
         }
         const uint32_t cn = min(32u, n - c);
         for (uint32_t j = 0; j < cn; j++) {
@@ -2272,7 +2278,7 @@ __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t ti
                     else hi = mid;
                 }
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
-                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx);
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx) >> a.wbits;
                 ck[k] = sm.c[lo];
             }
         }
@@ -2300,7 +2306,7 @@ __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
-            v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j)) : 0xffffffffu;
+            v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j) >> a.wbits) : 0xffffffffu;
         }
 #pragma unroll
         for (int k = 0; k < kUnroll; k++)

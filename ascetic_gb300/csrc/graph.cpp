@@ -197,7 +197,8 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     asc_budget_default(&def);
     if (!b) b = &def;
     const uint64_t E = g->E, V = g->V;
-    const uint64_t eb = 4ull * g->edge_words;
+    const uint64_t eb = 4ull * g->edge_words;       // device bytes per edge
+    const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : (double)eb;  // budget unit
     uint64_t frag = b->fragment_edges ? b->fragment_edges : 4096;
     uint64_t st = E;
     bool round_down = false;
@@ -207,8 +208,9 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
             break;
         case ASC_BUDGET_FRAC:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget fraction %g is negative", b->value);
-            if (b->value >= 1.0) st = E;
-            else { st = (uint64_t)(b->value * (double)E); round_down = true; }
+            // the fraction of the source edge-array bytes, spent on device-format edges
+            if (b->value * fb >= (double)eb) st = E;
+            else { st = (uint64_t)(b->value * (double)E * fb / (double)eb); round_down = true; }
             break;
         case ASC_BUDGET_BYTES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget bytes %g is negative", b->value);
@@ -274,9 +276,37 @@ static asc_status upload(asc_graph *g) {
     return ASC_OK;
 }
 
+// Weighted edges are packed into one u32, (dst << wbits) | weight, when the
+// destination needs at most 32 - wbits bits and every weight fits in wbits:
+// half the bytes per edge over the host link and twice the edges in the same
+// static-region bytes; values are unchanged. The AoS host copy is released.
+static asc_status pack_weighted(asc_graph *g) {
+    if (g->edge_words != 2) return ASC_OK;
+    uint32_t vbits = 1;
+    while (vbits < 32 && (1ull << vbits) < g->V) vbits++;
+    const uint32_t wbits = 32 - vbits;
+    if (wbits == 0 || (uint64_t)g->max_weight >= (1ull << wbits)) return ASC_OK;
+    uint32_t *packed = nullptr;
+    ASC_TRY(pinned_alloc((void **)&packed, sizeof(uint32_t) * (g->E ? g->E : 1)));
+    const uint32_t *aos = g->h_edges;
+    parallel_for(g->E, host_threads(g->E), [&](unsigned, uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; i++) packed[i] = (aos[2 * i] << wbits) | aos[2 * i + 1];
+    });
+    cudaFreeHost(g->h_edges);
+    g->h_edges = packed;
+    void *dp = nullptr;
+    ASC_CUDA(cudaHostGetDevicePointer(&dp, g->h_edges, 0));
+    g->d_host_edges = (const uint32_t *)dp;
+    g->edge_words = 1;
+    g->wbits = wbits;
+    return ASC_OK;
+}
+
 static asc_status finish_graph(asc_graph *g, const asc_budget *budget, asc_graph **out) {
     ASC_TRY(validate_and_measure(g));
-    ASC_TRY(compute_static_split(g, budget, g->is_csc ? 17 : (g->edge_words == 2 ? 15 : 13)));
+    g->file_edge_bytes = 4 * g->edge_words;
+    ASC_TRY(pack_weighted(g));
+    ASC_TRY(compute_static_split(g, budget, g->is_csc ? 17 : (g->file_edge_bytes == 8 ? 15 : 13)));
     ASC_TRY(upload(g));
     *out = g;
     return ASC_OK;
@@ -679,6 +709,7 @@ asc_status asc_graph_info_get(const asc_graph *g, asc_graph_info *info) {
     info->host_pinned_bytes = 4ull * g->edge_words * g->E;
     info->max_degree = g->max_degree;
     info->max_weight = g->max_weight;
+    info->weight_bits = g->wbits;
     return ASC_OK;
 }
 

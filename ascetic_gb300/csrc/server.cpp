@@ -405,7 +405,8 @@ asc_status asc_server_submit(asc_server *s, uint32_t graph_id, asc_algo algo, ui
     asc_graph *g = s->graphs[graph_id].g;
     if ((algo == ASC_BFS || algo == ASC_SSSP) && source >= g->V)
         return fail(ASC_ERR_INVALID, "source %u is not a vertex", source);
-    if (algo == ASC_SSSP && g->edge_words != 2) return fail(ASC_ERR_UNSUPPORTED, "SSSP needs a weighted graph");
+    if (algo == ASC_SSSP && g->edge_words != 2 && g->wbits == 0)
+        return fail(ASC_ERR_UNSUPPORTED, "SSSP needs a weighted graph");
     if ((algo == ASC_BFS || algo == ASC_SSSP || algo == ASC_CC) && g->is_csc)
         return fail(ASC_ERR_UNSUPPORTED, "BFS/SSSP/CC need an out-edge graph");
     if (algo > ASC_PR) return fail(ASC_ERR_INVALID, "unknown algorithm");

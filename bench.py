@@ -58,6 +58,7 @@ def parse():
                          "20,22,24,26 is the full serving configuration")
     ap.add_argument("--serve-queries", type=int, default=400)
     ap.add_argument("--serve-budget-gb", type=float, default=12.0)
+    ap.add_argument("--serve-sweep", type=int, default=1, help="run the Poisson rate sweep (0 skips it)")
     ap.add_argument("--pr-study", type=int, default=0,
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
@@ -279,7 +280,7 @@ def serve_leg(args):
     sweep = []
     cap = sf["queries_per_s"]
     n_sweep = min(len(plan), 120)
-    for frac in (0.5, 0.9, 2.0):
+    for frac in ((0.5, 0.9, 2.0) if args.serve_sweep else ()):
         rate = frac * cap
         b, _ = run(A.SERVE_BATCHED, rate=rate, n=n_sweep)
         f, _ = run(A.SERVE_FIFO, rate=rate, n=n_sweep)

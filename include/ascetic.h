@@ -64,7 +64,8 @@ typedef enum asc_algo { ASC_BFS = 0, ASC_SSSP = 1, ASC_CC = 2, ASC_PR = 3 } asc_
 
 typedef enum asc_budget_mode {
     ASC_BUDGET_ALL = 0,      /* whole edge array resident (no cap) */
-    ASC_BUDGET_FRAC = 1,     /* value = fraction of the edge-array bytes for the static region */
+    ASC_BUDGET_FRAC = 1,     /* value = fraction of the source edge-array bytes (4 or 8 per edge as in
+                                the file) for the static region */
     ASC_BUDGET_BYTES = 2,    /* value = bytes for the static region */
     ASC_BUDGET_ADVISE_K = 3, /* value = reference --adviseK: fraction of free device memory left
                                 after the vertex arrays (GraphMeta.cuh:310-354); 0 = its auto formula */
@@ -83,7 +84,7 @@ typedef struct asc_graph asc_graph;
 typedef struct asc_graph_info {
     uint64_t vertices;
     uint64_t edges;
-    uint32_t edge_bytes;          /* 4 (u32 destination) or 8 ({dst, weight}) */
+    uint32_t edge_bytes;          /* device/host bytes per edge: 4 (destination or packed) or 8 ({dst, weight}) */
     uint32_t is_csc;              /* 1 for .bcsc (in-edges + out-degree block) */
     uint64_t static_edges;        /* edges in the device-resident prefix */
     uint64_t static_vertices;     /* vertices [0, static_vertices) have every edge in the prefix */
@@ -92,6 +93,10 @@ typedef struct asc_graph_info {
     uint64_t host_pinned_bytes;   /* pinned host copy of the edge array (on-demand source) */
     uint32_t max_degree;
     uint32_t max_weight;          /* 0 for unweighted graphs */
+    uint32_t weight_bits;         /* > 0: weighted edges stored packed as (dst << bits) | weight in 4 bytes
+                                     (whenever destinations and weights fit): half the bytes per edge,
+                                     twice the edges in the same static-region bytes */
+    uint32_t reserved;
 } asc_graph_info;
 
 typedef enum asc_pr_mode {

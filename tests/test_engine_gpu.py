@@ -131,6 +131,28 @@ def test_batch_sssp_rows_equal_single_source(frac):
             assert np.array_equal(got[i], oracle.sssp(ptr, adj, s)), (frac, i, s)
 
 
+def test_packed_and_unpacked_weighted_edges():
+    """Weighted edges are stored packed (dst << bits | weight) when they fit,
+    AoS otherwise; both give the oracle's distances, and a byte budget holds
+    twice the edges when packed."""
+    ptr, adj = A.rmat_csr(13, 8, 36, weights=(1, 63))
+    big = adj.copy()
+    big[:, 1] = (big[:, 1].astype(np.uint64) * 40000).astype(np.uint32)   # needs > 19 weight bits
+    for arr, packed in ((adj, True), (big, False)):
+        with A.Graph.from_csr(ptr, arr, budget=A.make_budget(frac=0.2)) as g:
+            assert (g.info.weight_bits > 0) == packed
+            assert g.info.edge_bytes == (4 if packed else 8)
+            frac_edges = g.info.static_edges / g.E
+            assert (0.3 < frac_edges < 0.45) if packed else (0.1 < frac_edges < 0.22)
+            for s in (0, 41):
+                got, _ = g.run("sssp", s)
+                assert np.array_equal(got, oracle.sssp(ptr, arr, s)), (packed, s)
+                got, _ = g.run("bfs", s)
+                assert np.array_equal(got, oracle.bfs(ptr, arr[:, 0].copy(), s))
+            rows, _ = g.run_batch("sssp", [0, 41])
+            assert np.array_equal(rows[1], oracle.sssp(ptr, arr, 41))
+
+
 def test_cc_directed_is_min_ancestor():
     ptr, col = A.rmat_csr(12, 4, 14)
     with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.3)) as g:
