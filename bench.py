@@ -382,11 +382,17 @@ def main():
     dominant = "on-demand" if ms_o >= ms_s else "static"
     roof_static = {"kernel": "expand_kernel<BFS> static region", "bound": "hbm", "achieved": round(hbm_gbs, 1),
                    "peak": hbm_peak, "unit": "GB/s", "frac": round(hbm_gbs / hbm_peak, 4),
-                   "traffic": traffic.get("static"), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                   "traffic": (traffic.get("static") or {}).get("dram_bytes_per_launch"),
+                   "traffic_source": "profiles/traffic.json (ncu, DRAM read+write bytes per launch)",
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                    "ms_share": round(ms_s / (ms_s + ms_o), 3) if ms_s + ms_o else None}
     roof_link = {"kernel": "expand_kernel<BFS> on-demand region", "bound": "host-link",
                  "achieved": round(link_gbs, 1), "peak": round(dma_gbs, 1), "unit": "GB/s",
-                 "frac": round(link_gbs / dma_gbs, 4) if dma_gbs else None, "traffic": traffic.get("ondemand"),
+                 "frac": round(link_gbs / dma_gbs, 4) if dma_gbs else None,
+                 "traffic": (traffic.get("ondemand") or {}).get("dram_bytes_per_launch"),
+                 "link_traffic": (traffic.get("ondemand") or {}).get("link_bytes_per_launch"),
+                 "traffic_source": "profiles/traffic.json (ncu: DRAM read+write and host-link sector bytes per "
+                                   "on-demand launch)",
                  "peak_source": "pinned H2D cudaMemcpyAsync measured in this run",
                  "sm_zero_copy_read_peak": round(smread_gbs, 1),
                  "ms_share": round(ms_o / (ms_s + ms_o), 3) if ms_s + ms_o else None}
