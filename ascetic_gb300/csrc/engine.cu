@@ -741,19 +741,25 @@ struct PrSmem {
     uint32_t work;
 };
 
+// Reference mode walks the active set like a traversal frontier (list, or
+// the bitmap in id order when dense) and a vertex that stays active sets its
+// bit in the next bitmap; standard mode walks every vertex of the region.
 template <typename T, bool REF>
-__device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, PrSmem<T> &sm) {
+__device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, int mode, PrSmem<T> &sm,
+                        uint32_t *s_next) {
     const RegionArgs &a = p.r;
     const uint32_t i = tile * kBlock + threadIdx.x;
     bool valid;
     uint32_t u = 0;
-    if (a.q_in) {
+    if (mode == kList) {
         valid = i < n_in;
         if (valid) u = a.q_in[i];
     } else {
-        valid = a.dense_begin + i < a.dense_end;
         u = a.dense_begin + i;
+        valid = u < a.dense_end;
+        if (valid && mode == kBitmap) valid = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
     }
+    if (mode == kBitmap && !__syncthreads_or(valid)) return;
     uint32_t deg = 0, start = 0;
     bool huge = false;
     if (valid) {
@@ -768,7 +774,7 @@ __device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, PrSmem
     sm.start[threadIdx.x] = start;
     sm.sum[threadIdx.x] = (T)0;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
-    __syncthreads();
+    const uint32_t nact = __syncthreads_count(valid && !huge);
     const int lane = threadIdx.x & 31;
     for (uint32_t base = 0; base < total; base += kBlock) {
         const uint32_t e = base + threadIdx.x;
@@ -799,13 +805,15 @@ __device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, PrSmem
     double res = 0, dang = 0;
     bool won = false;
     if (valid && !huge) won = pr_apply<T, REF>(p, u, sm.sum[threadIdx.x], res, dang);
-    if (REF) push_warp(a, won, u);
-    if (!REF) block_reduce2_atomic<T>(res, dang, p.acc, sm.red);
+    if (REF) {
+        if (won) atomicOr(&a.bitmap[u >> 5], 1u << (u & 31));
+        count_next(a, won, u, s_next);
+    } else {
+        block_reduce2_atomic<T>(res, dang, p.acc, sm.red);
+    }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
-        uint32_t nv = a.q_in ? min(kBlock, n_in - tile * kBlock)
-                             : min((uint32_t)kBlock, a.dense_end - a.dense_begin - tile * kBlock);
-        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nv);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nact);
     }
     __syncthreads();
 }
@@ -838,12 +846,19 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
 template <typename T, bool REF>
 __global__ void __launch_bounds__(kBlock) pr_pull_kernel(PrArgs<T> p) {
     __shared__ PrSmem<T> sm;
+    __shared__ uint32_t s_next[2];
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     const RegionArgs &a = p.r;
-    const uint32_t n_in = a.q_in ? a.cnt_in[a.region] : 0;
-    const uint32_t nseg = a.cnt_in[2 + a.region];
-    const uint32_t nvert = a.q_in ? n_in : a.dense_end - a.dense_begin;
-    const uint32_t ntiles = (nvert + kBlock - 1) / kBlock;
-    const uint32_t total = nseg + ntiles;
+    uint32_t n_in, nseg, total;
+    int mode;
+    if (REF) {
+        region_items_bits(a, n_in, nseg, total, mode);
+    } else {
+        mode = kRange;
+        n_in = 0;
+        nseg = a.cnt_in[2 + a.region];
+        total = nseg + (a.dense_end - a.dense_begin + kBlock - 1) / kBlock;
+    }
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(a.work, 1u);
         __syncthreads();
@@ -851,8 +866,9 @@ __global__ void __launch_bounds__(kBlock) pr_pull_kernel(PrArgs<T> p) {
         __syncthreads();
         if (w >= total) break;
         if (w < nseg) pr_segment<T>(p, a.seg_in[w], sm);
-        else pr_tile<T, REF>(p, w - nseg, n_in, sm);
+        else pr_tile<T, REF>(p, w - nseg, n_in, mode, sm, s_next);
     }
+    if (REF) flush_next(a, s_next);
 }
 
 // Applies the segmented vertices once all their segments are summed. In
@@ -890,7 +906,15 @@ __global__ void pr_apply_segmented_kernel(PrArgs<T> p, const uint64_t *items_sta
                 won = pr_apply<T, REF>(p, v, s, res, dang);
             }
         }
-        if (REF) push_warp(a, won, v);
+        if (REF) {
+            // a long-list vertex that stays active joins the next bitmap
+            if (won) atomicOr(&a.bitmap[v >> 5], 1u << (v & 31));
+            const unsigned m0 = __ballot_sync(kFull, won && v < a.S), m1 = __ballot_sync(kFull, won && v >= a.S);
+            if ((threadIdx.x & 31) == 0) {
+                if (m0) atomicAdd(&a.cnt_out[6], (uint32_t)__popc(m0));
+                if (m1) atomicAdd(&a.cnt_out[7], (uint32_t)__popc(m1));
+            }
+        }
     }
     if (!REF) block_reduce2_atomic<T>(res, dang, p.acc, red);
 }
@@ -1431,9 +1455,13 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
                                                           acc + 2);
     launches++;
     RegionArgs sa = base_args(g, 1);  // seeds land in parity 0
+    const uint32_t nwords = V / 32 + 1;
     if (REF) {
-        seed_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(sa, 0, 1);
-        launches++;
+        // every vertex starts active: full bitmap, then lists/segments from it
+        for (int i = 0; i < 2; i++) ASC_CUDA(cudaMemsetAsync(ws->bitmap[i], 0, 4 * (V / 32 + 2), s));
+        seed_bits_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(sa, 0, 1, nwords);
+        build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(sa, ws->bitmap[0], nwords);
+        launches += 2;
     } else if (ws->n_huge_total) {
         seed_huge_segments_kernel<<<fill_grid(ws, ws->n_huge_total), kBlock, 0, s>>>(
             sa, ws->huge_list, ws->n_huge_static, ws->n_huge_total);
@@ -1442,18 +1470,18 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
     ASC_CUDA(cudaGetLastError());
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
-    uint32_t cnt[4];
+    uint32_t cnt[CTL_BLOCK];
     memcpy(cnt, ws->h_ctl, sizeof(cnt));
 
-    // REF: active lists alternate parity. STD: every vertex every pass (dense
-    // ranges) and the fixed segment list stays in parity 0.
+    // REF: the active set alternates parity like a traversal frontier. STD:
+    // every vertex every pass (dense ranges), fixed segment list in parity 0.
     int parity = 0;
     int it = 0;
     const int max_it = p.max_iterations > 0 ? p.max_iterations : (REF ? 1000000 : 100);
     double residual = 0;
     double phase_ms[2] = {0, 0};
     for (;;) {
-        if (REF && !(cnt[0] | cnt[1] | cnt[2] | cnt[3])) break;
+        if (REF && !(cnt[6] | cnt[7])) break;
         if (it >= max_it) {
             if (REF) return fail(ASC_ERR_TIMEOUT, "reference PageRank still active after %d passes", it);
             break;
@@ -1461,6 +1489,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         const int cp = it & 1;
         const int po = 1 - parity;
         ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
+        if (REF) ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
         if (!REF) ASC_CUDA(cudaMemsetAsync(acc + 2 * cp, 0, 16, s));
         PrArgs<T> pa;
         memset(&pa, 0, sizeof(pa));
@@ -1474,7 +1503,9 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         pa.dangling_prev = acc + 2 * (1 - cp) + 1;
         for (int region = 0; region < 2; region++) {
             RegionArgs a = region_args(g, parity, region, !REF);
-            const uint32_t nvert = REF ? cnt[region] : (region == 0 ? g->static_vertices : V - g->static_vertices);
+            const uint32_t range = region == 0 ? g->static_vertices : V - g->static_vertices;
+            const bool bitmap_mode = REF && ws->tune.dense_div && cnt[6 + region] > range / ws->tune.dense_div;
+            const uint32_t nvert = REF ? (bitmap_mode ? range : cnt[region]) : range;
             const uint64_t items = (uint64_t)cnt[2 + region] + (nvert + kBlock - 1) / kBlock;
             if (!items) continue;
             pa.r = a;
@@ -1491,8 +1522,14 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
                 pa, ws->segs[parity], ws->segs[parity] + ws->segcap_static, ws->huge_list, ws->n_huge_total);
             launches++;
         }
+        if (REF) {
+            build_frontier_kernel<<<fill_grid(ws, nwords), kBlock, 0, s>>>(region_args(g, parity, 0, false),
+                                                                            ws->bitmap[po], nwords);
+            launches++;
+        }
         ASC_CUDA(cudaGetLastError());
-        if (REF) ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 16, cudaMemcpyDeviceToHost, s));
+        if (REF)
+            ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, ws->ctl + CTL_BLOCK * po, 4 * CTL_BLOCK, cudaMemcpyDeviceToHost, s));
         else ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, acc + 2 * cp, 16, cudaMemcpyDeviceToHost, s));
         ASC_CUDA(cudaStreamSynchronize(s));
         if (pt.on) ASC_TRY(pt.sum(phase_ms));

@@ -298,3 +298,33 @@ def test_single_vertex_and_isolated_source():
         got, st = g.run("bfs", 0)
         assert got.tolist() == [1] + [11] * 9
         assert st["reached_vertices"] == 1 and st["reached_edges"] == 0
+
+
+def test_ptgraph_cli_matches_oracle():
+    """The drop-in command line: reference flags, values written with --output."""
+    import subprocess
+    d = tempfile.mkdtemp()
+    ptr, col = A.rmat_csr(12, 8, 37)
+    _, adj = A.rmat_csr(12, 8, 37, weights=(1, 63))
+    cptr, ccol, od = A.rmat_csr(12, 8, 37, transpose=True)
+    A.write_graph(os.path.join(d, "g.bcsr"), A.FMT_BCSR, ptr, col)
+    A.write_graph(os.path.join(d, "g.bwcsr"), A.FMT_BWCSR, ptr, adj)
+    A.write_graph(os.path.join(d, "g.bcsc"), A.FMT_BCSC, cptr, ccol, od)
+    cases = [("bfs", "g.bcsr", ["--source", "5"], oracle.bfs(ptr, col, 5)),
+             ("sssp", "g.bwcsr", ["--source", "5"], oracle.sssp(ptr, adj, 5)),
+             ("cc", "g.bcsr", [], oracle.cc(ptr, col)),
+             ("pr", "g.bcsc", [], oracle.pr_ref(cptr, ccol, od)[0])]
+    for algo, f, extra, exp in cases:
+        out = os.path.join(d, algo + ".out")
+        cmd = [A.PTGRAPH_PATH, "--input", os.path.join(d, f), "--type", algo, "--adviseK", "0.3",
+               "--method", "1", "--output", out, "--json", "1"] + extra
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        assert "move overload size" in r.stdout
+        got = np.fromfile(out, dtype=np.float64 if algo == "pr" else np.uint32)
+        if algo == "pr":
+            assert np.abs(got - exp).max() <= PR_TOL
+        else:
+            assert np.array_equal(got, exp), algo
+    r = subprocess.run([A.PTGRAPH_PATH, "--input", os.path.join(d, "missing.bcsr")], capture_output=True, text=True)
+    assert r.returncode == 2 and "bad graph file" in r.stderr
