@@ -21,6 +21,7 @@ from . import formats  # noqa: F401  (re-exported helper module)
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "libascetic_gb300.so")
 PTGRAPH_PATH = os.path.join(_PKG, "_lib", "ptgraph")
+CONVERT_PATH = os.path.join(_PKG, "_lib", "asc-convert")
 
 # enums (include/ascetic.h)
 OK, ERR_INVALID, ERR_BAD_FILE, ERR_BUDGET, ERR_CUDA, ERR_TIMEOUT, ERR_CANCELLED, ERR_UNSUPPORTED, \

@@ -1,5 +1,6 @@
-"""Builds the engine in-tree: ascetic_gb300/_lib/libascetic_gb300.so and the
-ptgraph command line, for sm_103a only (nvcc, no torch extension machinery).
+"""Builds the engine in-tree: ascetic_gb300/_lib/libascetic_gb300.so, the
+ptgraph command line and the asc-convert file converter, for sm_103a only
+(nvcc, no torch extension machinery).
 
 The translation units compile in parallel; nothing is fetched or installed.
 """
@@ -19,6 +20,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libascetic_gb300.so")
 PTGRAPH_PATH = os.path.join(LIB_DIR, "ptgraph")
+CONVERT_PATH = os.path.join(LIB_DIR, "asc-convert")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["engine.cu", "graph.cpp", "capi.cpp", "server.cpp"]
@@ -76,12 +78,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB_PATH + ".tmp%d" % os.getpid()
         run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB_PATH)
-    cli_src = os.path.join(CSRC, "ptgraph.cpp")
-    if force or _stale(PTGRAPH_PATH, [cli_src, LIB_PATH] + headers):
-        tmp = PTGRAPH_PATH + ".tmp%d" % os.getpid()
-        run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", tmp, "-L" + LIB_DIR,
-             "-lascetic_gb300", "-Wl,-rpath,$ORIGIN"])
-        os.replace(tmp, PTGRAPH_PATH)
+    for exe, src in ((PTGRAPH_PATH, "ptgraph.cpp"), (CONVERT_PATH, "convert.cpp")):
+        cli_src = os.path.join(CSRC, src)
+        if force or _stale(exe, [cli_src, LIB_PATH] + headers):
+            tmp = exe + ".tmp%d" % os.getpid()
+            run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, cli_src, "-o", tmp, "-L" + LIB_DIR,
+                 "-lascetic_gb300", "-Wl,-rpath,$ORIGIN"])
+            os.replace(tmp, exe)
     return LIB_PATH
 
 

@@ -162,3 +162,54 @@ def relax_mt(mode, ptr, edges, src, nthreads):
     _check(_load().orc_relax_mt(mode, V, ptr, edges if len(edges) else np.zeros(2, np.uint32), src,
                                 nthreads, out, ctypes.byref(it)), "relax_mt")
     return out[:V], it.value
+
+
+def converter(src, dst, by_dst=False, compat=False):
+    """The reference converter's CSR/CSC build, restated (converter/converter.cpp).
+
+    V = largest id + 1 over both endpoints (converter.cpp:102-125); offsets are
+    the running degree sum, stepped back by one once it reaches E
+    (converter.cpp:131-138) when ``compat``; each list keeps the edges in input
+    order (converter.cpp:143-164; :246-268 for CSC, keyed by destination and
+    storing the source). Pure Python loops: small inputs only. Returns
+    (V, ptr uint64[V+1] with ptr[V] = E, order int64[E] = input index of each
+    placed edge, outdeg uint32[V]).
+    """
+    src = [int(x) for x in src]
+    dst = [int(x) for x in dst]
+    E = len(src)
+    V = max([max(s, d) + 1 for s, d in zip(src, dst)] or [0])
+    key = dst if by_dst else src
+    deg = [0] * V
+    for k in key:
+        deg[k] += 1
+    ptr = [0] * (V + 1)
+    t = 0
+    for v in range(V):
+        ptr[v] = t
+        t += deg[v]
+        if compat and t == E and E:
+            t -= 1
+    ptr[V] = E
+    exact = [0] * V
+    t = 0
+    for v in range(V):
+        exact[v] = t
+        t += deg[v]
+    anchor = [0] * V
+    order = [0] * E
+    for i, k in enumerate(key):
+        order[exact[k] + anchor[k]] = i
+        anchor[k] += 1
+    outdeg = [0] * V
+    for s in src:
+        outdeg[s] += 1
+    return V, np.array(ptr, np.uint64), np.array(order, np.int64), np.array(outdeg, np.uint32)
+
+
+def converter_ref_weights(n):
+    """convertByteToBWCSR's weights (converter.cpp:303-306, :396): srand(0), then
+    rand() % 20 per edge in input order, drawn from this host's C library."""
+    libc = ctypes.CDLL(None)
+    libc.srand(0)
+    return np.array([libc.rand() % 20 for _ in range(n)], np.uint32)
