@@ -28,7 +28,7 @@ OK, ERR_INVALID, ERR_BAD_FILE, ERR_BUDGET, ERR_CUDA, ERR_TIMEOUT, ERR_CANCELLED,
     ERR_NO_DEVICE, ERR_NOMEM, ERR_BUSY = range(11)
 FMT_AUTO, FMT_BCSR, FMT_BWCSR, FMT_BCSC, FMT_BCSR32 = range(5)
 BFS, SSSP, CC, PR = range(4)
-BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES = range(5)
+BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES, BUDGET_MANAGED = range(6)
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
 RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP = 1, 2, 4, 8
@@ -43,7 +43,7 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
             "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
             "asc_server_stats_get", "asc_server_destroy", "asc_graph_get_tuning", "asc_graph_set_tuning",
-            "asc_graph_tune"]
+            "asc_graph_tune", "asc_device_memory"]
 TUNE_NO_CACHE = 1
 SERVE_BATCHED, SERVE_FIFO = 0, 1
 
@@ -68,7 +68,7 @@ class GraphInfo(ctypes.Structure):
                 ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
                 ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32),
-                ("weight_bits", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("weight_bits", ctypes.c_uint32), ("edge_bits", ctypes.c_uint32)]
 
 
 class Tuning(ctypes.Structure):
@@ -145,6 +145,7 @@ def lib():
         "asc_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
         "asc_version": ([], ctypes.c_char_p),
         "asc_device_count": ([], ctypes.c_int),
+        "asc_device_memory": ([P(c_u64), P(c_u64)], ctypes.c_int),
         "asc_budget_default": ([P(Budget)], None),
         "asc_graph_open": ([ctypes.c_char_p, ctypes.c_int, P(Budget), gpp], ctypes.c_int),
         "asc_graph_from_csr": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, P(Budget), gpp], ctypes.c_int),
@@ -199,11 +200,21 @@ def device_count():
     return lib().asc_device_count()
 
 
-def make_budget(frac=None, nbytes=None, edges=None, advise_k=None, fragment_edges=4096):
+def device_free_bytes():
+    free, total = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(lib().asc_device_memory(ctypes.byref(free), ctypes.byref(total)))
+    return free.value
+
+
+def make_budget(frac=None, nbytes=None, edges=None, advise_k=None, fragment_edges=4096, managed=False):
+    """Static-region budget. managed=True selects the UVM comparison engine
+    (no static region, edges in CUDA managed memory)."""
     b = Budget()
     lib().asc_budget_default(ctypes.byref(b))
     b.fragment_edges = fragment_edges
-    if frac is not None:
+    if managed:
+        b.mode, b.value = BUDGET_MANAGED, 0.0
+    elif frac is not None:
         b.mode, b.value = BUDGET_FRAC, float(frac)
     elif nbytes is not None:
         b.mode, b.value = BUDGET_BYTES, float(nbytes)

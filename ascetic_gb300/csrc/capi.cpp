@@ -100,6 +100,14 @@ int asc_device_count(void) {
     return n;
 }
 
+asc_status asc_device_memory(uint64_t *free_bytes, uint64_t *total_bytes) {
+    size_t f = 0, t = 0;
+    ASC_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return ASC_OK;
+}
+
 void asc_params_default(asc_params *p) {
     if (!p) return;
     memset(p, 0, sizeof(*p));

@@ -79,16 +79,19 @@ struct asc_graph {
     uint64_t V = 0, E = 0;
     uint32_t edge_words = 1;      // 1: u32 destination (or packed dst/weight), 2: {dst, weight}
     uint32_t wbits = 0;           // > 0: weighted edges packed as (dst << wbits) | weight in one u32
+    uint32_t ebits = 32;          // edge_words == 1: bits per edge word in h_edges / d_static (< 32:
+                                  // a bit stream, edge i at bits [i*ebits, (i+1)*ebits))
     uint32_t file_edge_bytes = 4; // bytes per edge of the source layout (the budget's unit)
     bool is_csc = false;
     uint32_t max_degree = 0;
     uint32_t max_weight = 0;
     // host (pinned)
     uint32_t *h_ptr = nullptr;    // V+1 offsets (u32: E < 2^32)
-    uint32_t *h_edges = nullptr;  // E * edge_words, mapped for device reads
+    uint32_t *h_edges = nullptr;  // E * edge_words (or the ebits stream), mapped for device reads
     uint32_t *h_outdeg = nullptr; // V (CSC graphs)
     // device
     const uint32_t *d_host_edges = nullptr;  // device address of h_edges (zero-copy reads)
+    uint32_t *managed_edges = nullptr;       // ASC_BUDGET_MANAGED: managed copy read instead
     uint32_t *d_ptr = nullptr;
     uint32_t *d_static = nullptr;  // edge prefix [0, static_edges)
     uint32_t *d_outdeg = nullptr;
@@ -103,6 +106,18 @@ struct asc_graph {
 };
 
 namespace asc {
+// u32 words holding edges [0, n) of a graph's edge array (plus one word of
+// padding for bit streams, so a straddling read never leaves the buffer)
+inline uint64_t edge_store_words(const asc_graph *g, uint64_t n) {
+    if (g->edge_words == 2) return 2 * n;
+    if (g->ebits == 32) return n;
+    return (n * g->ebits + 31) / 32 + 1;
+}
+// bytes that n edges occupy in the stored layout (what n on-demand edges move over the link)
+inline uint64_t edge_store_bytes(const asc_graph *g, uint64_t n) {
+    if (g->edge_words == 2) return 8 * n;
+    return (n * g->ebits + 7) / 8;
+}
 // engine.cu
 asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
                          asc_stats *st);

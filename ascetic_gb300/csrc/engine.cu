@@ -91,12 +91,47 @@ struct RegionArgs {
     uint32_t V;
     uint32_t dense_div;
     uint32_t wbits;               // > 0: u32 edges packed as (dst << wbits) | weight
+    uint32_t ebits;               // bits per stored edge word: 32, or a bit stream of ebits per edge
 };
 
-// How a tile picks its vertices: from the frontier list, every vertex of a
-// range, or the vertices of a range whose frontier bit is set (id order, so
-// the lists of neighbouring active vertices are read as one contiguous run).
-enum TileMode { kList = 0, kRange = 1, kBitmap = 2 };
+// Edge layouts of the expansion kernels (their WORDS template argument):
+// 1 = one u32 per edge, 2 = {dst, weight} pairs, kBitsLayout = one word per
+// edge stored as a bit stream of ebits per edge.
+constexpr int kBitsLayout = 3;
+
+// ebits bits of a bit stream: edge idx at bits [idx*ebits, (idx+1)*ebits),
+// little-endian across words; the buffer carries a padding word, so p[1]
+// stays inside it.
+__device__ __forceinline__ uint32_t bit_stream_word(const uint32_t *base, uint64_t idx, uint32_t ebits) {
+    const uint64_t bit = idx * ebits;
+    const uint32_t *p = base + (bit >> 5);
+    const uint32_t sh = (uint32_t)bit & 31u;
+    uint32_t x = __ldg(p) >> sh;
+    if (sh + ebits > 32) x |= __ldg(p + 1) << (32 - sh);
+    return x & ((1u << ebits) - 1u);
+}
+
+template <int WORDS>
+__device__ __forceinline__ uint32_t layout_word(const uint32_t *base, uint64_t idx, uint32_t ebits) {
+    return WORDS == kBitsLayout ? bit_stream_word(base, idx, ebits) : __ldg(base + idx);
+}
+
+// Edge word idx of a one-word-per-edge array: a plain load, or a bit-stream
+// read when ebits < 32 (kernels with the layout as a template argument call
+// bit_stream_word directly, without the per-edge test).
+__device__ __forceinline__ uint32_t edge_word(const uint32_t *base, uint64_t idx, uint32_t ebits) {
+    if (ebits == 32) return __ldg(base + idx);
+    const uint64_t bit = idx * ebits;
+    const uint32_t *p = base + (bit >> 5);
+    const uint32_t sh = (uint32_t)bit & 31u;
+    uint32_t x = __ldg(p) >> sh;
+    if (sh + ebits > 32) x |= __ldg(p + 1) << (32 - sh);
+    return x & ((1u << ebits) - 1u);
+}
+
+// How a PageRank tile picks its vertices: from the active list, or every
+// vertex of a range (frontiers walked through their bitmap use chunks).
+enum TileMode { kList = 0, kRange = 1 };
 
 struct Smem {
     uint32_t pref[kBlock + 1];
@@ -179,7 +214,7 @@ __device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint
         v = e.x;
         nv = ALG == kSSSP ? vu + e.y : (ALG == kBFS ? vu + 1 : vu);
     } else {
-        const uint32_t e = __ldg(a.edges + idx);
+        const uint32_t e = layout_word<WORDS>(a.edges, idx, a.ebits);
         v = e >> a.wbits;
         nv = ALG == kBFS ? vu + 1 : (ALG == kSSSP ? vu + (e & ((1u << a.wbits) - 1u)) : vu);
     }
@@ -232,21 +267,11 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
 // kUnroll independent reads in flight (on-demand column reads cross the host link).
 constexpr int kUnroll = 4;
 
+// Expands up to kBlock frontier vertices, one per thread (act = false where a
+// thread has none): a block scan of their degrees lays the edges out as one
+// range, which all threads walk kUnroll edges at a time.
 template <int ALG, int WORDS>
-__device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, Smem &sm,
-                            uint32_t *s_next) {
-    const uint32_t i = tile * kBlock + threadIdx.x;
-    bool act;
-    uint32_t u;
-    if (mode == kList) {
-        act = i < n_in;
-        u = act ? a.q_in[i] : 0;
-    } else {
-        u = a.dense_begin + i;
-        act = u < a.dense_end;
-        if (act && mode == kBitmap) act = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
-    }
-    if (mode == kBitmap && !__syncthreads_or(act)) return;  // no active vertex in this id range
+__device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem &sm, uint32_t *s_next) {
     uint32_t deg = 0, start = 0, vu = 0;
     if (act) {
         start = a.ptr[u];
@@ -305,6 +330,37 @@ __device__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, i
     __syncthreads();
 }
 
+// One bitmap word of a region walked through its bitmap, bits outside
+// [dense_begin, dense_end) cleared (u0 is 32-aligned).
+__device__ __forceinline__ uint32_t region_word(const RegionArgs &a, uint32_t u0) {
+    if (u0 >= a.dense_end) return 0u;
+    uint32_t word = a.bitmap_in[u0 >> 5];
+    if (u0 < a.dense_begin) word &= 0xffffffffu << (a.dense_begin - u0);
+    if (a.dense_end - u0 < 32u) word &= (1u << (a.dense_end - u0)) - 1u;
+    return word;
+}
+
+// One tile of frontier vertices, one per thread: kBlock consecutive entries
+// of the region's list, or (bitmap) kBlock consecutive vertex ids walked
+// through the frontier bitmap (tiles start 32-aligned; a tile with no active
+// vertex costs one bitmap read per warp).
+template <int ALG, int WORDS>
+__device__ __forceinline__ void expand_tile(const RegionArgs &a, uint32_t tile, uint32_t n_in, bool bitmap, Smem &sm,
+                                            uint32_t *s_next) {
+    bool act;
+    uint32_t u;
+    if (bitmap) {
+        u = (a.dense_begin & ~31u) + tile * kBlock + threadIdx.x;
+        act = (region_word(a, u & ~31u) >> (u & 31)) & 1u;
+        if (!__syncthreads_or(act)) return;
+    } else {
+        const uint32_t i = tile * kBlock + threadIdx.x;
+        act = i < n_in;
+        u = act ? a.q_in[i] : 0;
+    }
+    expand_vertices<ALG, WORDS>(a, act, u, sm, s_next);
+}
+
 template <int ALG, int WORDS>
 __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_next) {
     const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
@@ -343,35 +399,27 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
     }
 }
 
-__device__ __forceinline__ void region_items(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg, uint32_t &items,
-                                             int &mode) {
-    n_in = a.q_in ? a.cnt_in[a.region] : 0;
-    nseg = a.cnt_in[2 + a.region];
-    const uint32_t range = a.dense_end - a.dense_begin;
-    if (!a.q_in) mode = kRange;
-    else if (a.bitmap_in && a.dense_div && n_in > range / a.dense_div) mode = kBitmap;
-    else mode = kList;
-    const uint32_t nvert = mode == kList ? n_in : range;
-    items = nseg + (nvert + kBlock - 1) / kBlock;
-}
-
-// Work of one region for the bitmap-built frontier: a region whose frontier
-// holds more than 1/dense_div of its vertices is walked through the bitmap in
-// id order (its list was not built), otherwise through its list.
+// Work of one region for the bitmap-built frontier: segments first, then a
+// region whose frontier holds more than 1/dense_div of its vertices is walked
+// in id order through its bitmap (its list was not built), kBlock ids per
+// item, so the lists of neighbouring active vertices are read as one
+// contiguous run; otherwise through its list, kBlock entries per item.
 __device__ __forceinline__ void region_items_bits(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg,
-                                                  uint32_t &items, int &mode) {
+                                                  uint32_t &items, bool &bitmap) {
     const uint32_t range = a.dense_end - a.dense_begin;
     const uint32_t bits = a.cnt_in[6 + a.region];
     nseg = a.cnt_in[2 + a.region];
-    if (a.bitmap_in && a.dense_div && bits > range / a.dense_div) {
-        mode = kBitmap;
-        n_in = 0;
-    } else {
-        mode = kList;
-        n_in = a.cnt_in[a.region];
-    }
-    const uint32_t nvert = mode == kList ? n_in : range;
+    bitmap = a.bitmap_in && a.dense_div && bits > range / a.dense_div;
+    n_in = bitmap ? 0 : a.cnt_in[a.region];
+    const uint32_t nvert = bitmap ? a.dense_end - (a.dense_begin & ~31u) : n_in;
     items = nseg + (nvert + kBlock - 1) / kBlock;
+}
+
+template <int ALG, int WORDS>
+__device__ __forceinline__ void expand_item(const RegionArgs &a, uint32_t w, uint32_t n_in, uint32_t nseg,
+                                            bool bitmap, Smem &sm, uint32_t *s_next) {
+    if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w], s_next);
+    else expand_tile<ALG, WORDS>(a, w - nseg, n_in, bitmap, sm, s_next);
 }
 
 __device__ __forceinline__ void flush_next(const RegionArgs &a, uint32_t *s_next) {
@@ -388,16 +436,15 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_kernel(R
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     uint32_t n_in, nseg, total;
-    int mode;
-    region_items_bits(a, n_in, nseg, total, mode);
+    bool bitmap;
+    region_items_bits(a, n_in, nseg, total, bitmap);
     for (;;) {
         if (threadIdx.x == 0) sm.work = atomicAdd(a.work, 1u);
         __syncthreads();
         const uint32_t w = sm.work;
         __syncthreads();
         if (w >= total) break;
-        if (w < nseg) expand_segment<ALG, WORDS>(a, a.seg_in[w], s_next);
-        else expand_tile<ALG, WORDS>(a, w - nseg, n_in, mode, sm, s_next);
+        expand_item<ALG, WORDS>(a, w, n_in, nseg, bitmap, sm, s_next);
     }
     flush_next(a, s_next);
 }
@@ -417,7 +464,7 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     uint32_t n0, s0, i0, n1, s1, i1;
-    int m0, m1;
+    bool m0, m1;
     region_items_bits(x.r0, n0, s0, i0, m0);
     region_items_bits(x.r1, n1, s1, i1, m1);
     const uint32_t m = min(i0, i1), total = i0 + i1;
@@ -436,13 +483,8 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
             od = i1 > i0;
             local = m + (w - 2 * m);
         }
-        if (od) {
-            if (local < s1) expand_segment<ALG, WORDS>(x.r1, x.r1.seg_in[local], s_next);
-            else expand_tile<ALG, WORDS>(x.r1, local - s1, n1, m1, sm, s_next);
-        } else {
-            if (local < s0) expand_segment<ALG, WORDS>(x.r0, x.r0.seg_in[local], s_next);
-            else expand_tile<ALG, WORDS>(x.r0, local - s0, n0, m0, sm, s_next);
-        }
+        if (od) expand_item<ALG, WORDS>(x.r1, local, n1, s1, m1, sm, s_next);
+        else expand_item<ALG, WORDS>(x.r0, local, n0, s0, m0, sm, s_next);
     }
     flush_next(x.r0, s_next);
 }
@@ -745,21 +787,8 @@ struct PrSmem {
 // the bitmap in id order when dense) and a vertex that stays active sets its
 // bit in the next bitmap; standard mode walks every vertex of the region.
 template <typename T, bool REF>
-__device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, int mode, PrSmem<T> &sm,
-                        uint32_t *s_next) {
+__device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T> &sm, uint32_t *s_next) {
     const RegionArgs &a = p.r;
-    const uint32_t i = tile * kBlock + threadIdx.x;
-    bool valid;
-    uint32_t u = 0;
-    if (mode == kList) {
-        valid = i < n_in;
-        if (valid) u = a.q_in[i];
-    } else {
-        u = a.dense_begin + i;
-        valid = u < a.dense_end;
-        if (valid && mode == kBitmap) valid = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
-    }
-    if (mode == kBitmap && !__syncthreads_or(valid)) return;
     uint32_t deg = 0, start = 0;
     bool huge = false;
     if (valid) {
@@ -788,7 +817,7 @@ __device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, int mo
                 else hi = mid;
             }
             owner = lo;
-            const uint32_t srcv = __ldg(a.edges + (uint64_t)sm.start[lo] + (e - sm.pref[lo]));
+            const uint32_t srcv = edge_word(a.edges, (uint64_t)sm.start[lo] + (e - sm.pref[lo]), a.ebits);
             x = p.c_old[srcv];
         }
         // segmented suffix sum over lanes with the same owner (owners ascend with the lane)
@@ -818,6 +847,30 @@ __device__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, int mo
     __syncthreads();
 }
 
+template <typename T, bool REF>
+__device__ __forceinline__ void pr_tile(const PrArgs<T> &p, uint32_t tile, uint32_t n_in, int mode, PrSmem<T> &sm,
+                                        uint32_t *s_next) {
+    const RegionArgs &a = p.r;
+    const uint32_t i = tile * kBlock + threadIdx.x;
+    bool valid;
+    uint32_t u = 0;
+    if (mode == kList) {
+        valid = i < n_in;
+        if (valid) u = a.q_in[i];
+    } else {
+        u = a.dense_begin + i;
+        valid = u < a.dense_end;
+    }
+    pr_vertices<T, REF>(p, valid, u, sm, s_next);
+}
+
+template <typename T, bool REF>
+__device__ void pr_bitmap_tile(const PrArgs<T> &p, uint32_t tile, PrSmem<T> &sm, uint32_t *s_next) {
+    const uint32_t u = (p.r.dense_begin & ~31u) + tile * kBlock + threadIdx.x;
+    const bool valid = (region_word(p.r, u & ~31u) >> (u & 31)) & 1u;
+    if (__syncthreads_or(valid)) pr_vertices<T, REF>(p, valid, u, sm, s_next);
+}
+
 template <typename T>
 __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
     const RegionArgs &a = p.r;
@@ -827,7 +880,7 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     T x = (T)0;
-    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += p.c_old[__ldg(a.edges + b + j)];
+    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += p.c_old[edge_word(a.edges, b + j, a.ebits)];
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(kFull, x, d);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -850,11 +903,10 @@ __global__ void __launch_bounds__(kBlock) pr_pull_kernel(PrArgs<T> p) {
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     const RegionArgs &a = p.r;
     uint32_t n_in, nseg, total;
-    int mode;
+    bool bitmap = false;
     if (REF) {
-        region_items_bits(a, n_in, nseg, total, mode);
+        region_items_bits(a, n_in, nseg, total, bitmap);
     } else {
-        mode = kRange;
         n_in = 0;
         nseg = a.cnt_in[2 + a.region];
         total = nseg + (a.dense_end - a.dense_begin + kBlock - 1) / kBlock;
@@ -866,7 +918,8 @@ __global__ void __launch_bounds__(kBlock) pr_pull_kernel(PrArgs<T> p) {
         __syncthreads();
         if (w >= total) break;
         if (w < nseg) pr_segment<T>(p, a.seg_in[w], sm);
-        else pr_tile<T, REF>(p, w - nseg, n_in, mode, sm, s_next);
+        else if (REF && bitmap) pr_bitmap_tile<T, REF>(p, w - nseg, sm, s_next);
+        else pr_tile<T, REF>(p, w - nseg, n_in, REF ? kList : kRange, sm, s_next);
     }
     if (REF) flush_next(a, s_next);
 }
@@ -1047,6 +1100,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.huge_bits = ws->huge_bits;
     a.dense_div = ws->tune.dense_div;
     a.wbits = g->wbits;
+    a.ebits = g->edge_words == 1 ? g->ebits : 32;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
     a.huge = ws->tune.huge_degree;
@@ -1128,16 +1182,29 @@ void launch_fused(cudaStream_t s, const FusedArgs &x, uint32_t grid) {
     expand_fused_kernel<ALG, WORDS><<<grid, kBlock, 0, s>>>(x);
 }
 
-FusedFn pick_fused(asc_algo algo, uint32_t words) {
-    if (algo == ASC_BFS) return words == 2 ? launch_fused<kBFS, 2> : launch_fused<kBFS, 1>;
-    if (algo == ASC_CC) return words == 2 ? launch_fused<kCC, 2> : launch_fused<kCC, 1>;
-    return words == 2 ? launch_fused<kSSSP, 2> : launch_fused<kSSSP, 1>;
+// the expansion kernels' WORDS argument for a graph's stored edge layout
+int edge_layout(const asc_graph *g) { return g->edge_words == 2 ? 2 : (g->ebits < 32 ? kBitsLayout : 1); }
+
+FusedFn pick_fused(asc_algo algo, int layout) {
+    if (algo == ASC_BFS)
+        return layout == 2 ? launch_fused<kBFS, 2> : layout == kBitsLayout ? launch_fused<kBFS, kBitsLayout>
+                                                                            : launch_fused<kBFS, 1>;
+    if (algo == ASC_CC)
+        return layout == 2 ? launch_fused<kCC, 2> : layout == kBitsLayout ? launch_fused<kCC, kBitsLayout>
+                                                                           : launch_fused<kCC, 1>;
+    return layout == 2 ? launch_fused<kSSSP, 2> : layout == kBitsLayout ? launch_fused<kSSSP, kBitsLayout>
+                                                                         : launch_fused<kSSSP, 1>;
 }
 
-ExpandFn pick_expand(asc_algo algo, uint32_t words) {
-    if (algo == ASC_BFS) return words == 2 ? launch_expand<kBFS, 2> : launch_expand<kBFS, 1>;
-    if (algo == ASC_CC) return words == 2 ? launch_expand<kCC, 2> : launch_expand<kCC, 1>;
-    return words == 2 ? launch_expand<kSSSP, 2> : launch_expand<kSSSP, 1>;
+ExpandFn pick_expand(asc_algo algo, int layout) {
+    if (algo == ASC_BFS)
+        return layout == 2 ? launch_expand<kBFS, 2> : layout == kBitsLayout ? launch_expand<kBFS, kBitsLayout>
+                                                                             : launch_expand<kBFS, 1>;
+    if (algo == ASC_CC)
+        return layout == 2 ? launch_expand<kCC, 2> : layout == kBitsLayout ? launch_expand<kCC, kBitsLayout>
+                                                                            : launch_expand<kCC, 1>;
+    return layout == 2 ? launch_expand<kSSSP, 2> : layout == kBitsLayout ? launch_expand<kSSSP, kBitsLayout>
+                                                                          : launch_expand<kSSSP, 1>;
 }
 
 // Per-iteration phase timing with events on the engine's stream.
@@ -1187,7 +1254,7 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
         cudaGraphExecDestroy(ws->loop_exec[slot]);
         ws->loop_exec[slot] = nullptr;
     }
-    FusedFn fused = pick_fused(algo, g->edge_words);
+    FusedFn fused = pick_fused(algo, edge_layout(g));
     const uint32_t V = (uint32_t)g->V;
     const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
     cudaGraph_t graph = nullptr;
@@ -1288,8 +1355,8 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     const bool all = algo == ASC_CC;
     uint32_t launches = 0;
     PhaseTimer pt(ws, (p.flags & ASC_RUN_PHASE_TIMING) != 0);
-    ExpandFn expand = pick_expand(algo, g->edge_words);
-    FusedFn fused = pick_fused(algo, g->edge_words);
+    ExpandFn expand = pick_expand(algo, edge_layout(g));
+    FusedFn fused = pick_fused(algo, edge_layout(g));
 
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
@@ -1413,7 +1480,7 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         st->iterations = iters;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         if (algo == ASC_CC) {
@@ -1556,7 +1623,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         st->iterations = it;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = hs[1] * 4ull;
+        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         st->reached_vertices = V;
@@ -1650,19 +1717,7 @@ __device__ __forceinline__ void mark_touched(const MsArgs &m, bool first, uint32
 }
 
 template <int WORDS>
-__device__ void ms_tile(const MsArgs &m, const RegionArgs &a, uint32_t tile, uint32_t n_in, int mode, MsSmem &sm) {
-    const uint32_t i = tile * kBlock + threadIdx.x;
-    bool act;
-    uint32_t u;
-    if (mode == kList) {
-        act = i < n_in;
-        u = act ? a.q_in[i] : 0;
-    } else {
-        u = a.dense_begin + i;
-        act = u < a.dense_end;
-        if (act && mode == kBitmap) act = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
-    }
-    if (mode == kBitmap && !__syncthreads_or(act)) return;
+__device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint32_t u, MsSmem &sm) {
     uint32_t deg = 0, start = 0;
     unsigned long long f = 0;
     if (act) {
@@ -1697,7 +1752,7 @@ __device__ void ms_tile(const MsArgs &m, const RegionArgs &a, uint32_t tile, uin
                     else hi = mid;
                 }
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
-                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx) >> a.wbits;
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : layout_word<WORDS>(a.edges, idx, a.ebits) >> a.wbits;
                 fk[k] = sm.f[lo];
             }
         }
@@ -1729,7 +1784,8 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
             ok[k] = j < n;
-            v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j) >> a.wbits) : 0;
+            v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : layout_word<WORDS>(a.edges, b + j, a.ebits) >> a.wbits)
+                         : 0;
         }
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
@@ -1743,10 +1799,26 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
 }
 
 template <int WORDS>
+__device__ __forceinline__ void ms_item(const MsArgs &m, const RegionArgs &a, uint32_t w, uint32_t n_in,
+                                        uint32_t nseg, bool bitmap, MsSmem &sm) {
+    if (w < nseg) {
+        ms_segment<WORDS>(m, a, a.seg_in[w]);
+    } else if (!bitmap) {
+        const uint32_t i = (w - nseg) * kBlock + threadIdx.x;
+        const bool act = i < n_in;
+        ms_vertices<WORDS>(m, a, act, act ? a.q_in[i] : 0, sm);
+    } else {
+        const uint32_t u = (a.dense_begin & ~31u) + (w - nseg) * kBlock + threadIdx.x;
+        const bool act = (region_word(a, u & ~31u) >> (u & 31)) & 1u;
+        if (__syncthreads_or(act)) ms_vertices<WORDS>(m, a, act, u, sm);
+    }
+}
+
+template <int WORDS>
 __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
     __shared__ MsSmem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
-    int m0, m1;
+    bool m0, m1;
     region_items_bits(m.r0, n0, s0, i0, m0);
     region_items_bits(m.r1, n1, s1, i1, m1);
     const uint32_t mm = min(i0, i1), total = i0 + i1;
@@ -1765,13 +1837,8 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
             od = i1 > i0;
             local = mm + (w - 2 * mm);
         }
-        if (od) {
-            if (local < s1) ms_segment<WORDS>(m, m.r1, m.r1.seg_in[local]);
-            else ms_tile<WORDS>(m, m.r1, local - s1, n1, m1, sm);
-        } else {
-            if (local < s0) ms_segment<WORDS>(m, m.r0, m.r0.seg_in[local]);
-            else ms_tile<WORDS>(m, m.r0, local - s0, n0, m0, sm);
-        }
+        if (od) ms_item<WORDS>(m, m.r1, local, n1, s1, m1, sm);
+        else ms_item<WORDS>(m, m.r0, local, n0, s0, m0, sm);
     }
 }
 
@@ -1791,7 +1858,7 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
         uint32_t ev = 0, ew = 0;
         if (c + lane < n) {
             if (a.wbits) {
-                const uint32_t e = __ldg(a.edges + b + c + lane);
+                const uint32_t e = edge_word(a.edges, b + c + lane, a.ebits);
                 ev = e >> a.wbits;
                 ew = e & ((1u << a.wbits) - 1u);
             } else {
@@ -1801,22 +1868,37 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
             }
         }
         const uint32_t cn = min(32u, n - c);
-        for (uint32_t j = 0; j < cn; j++) {
-            const uint32_t v = __shfl_sync(kFull, ev, j);
-            const uint32_t w = __shfl_sync(kFull, ew, j);
-            uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
-            bool imp_lo = false, imp_hi = false;
-            if (lo_on) {
-                const uint32_t nd = d_lo + w;
-                if (nd < row[lane]) imp_lo = nd < atomicMin(&row[lane], nd);
+        // four edges at a time: their distance-row reads are in flight together
+        for (uint32_t j0 = 0; j0 < cn; j0 += 4) {
+            uint32_t vv[4], ww[4], clo[4], chi[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const uint32_t j = j0 + k;
+                vv[k] = __shfl_sync(kFull, ev, j & 31);
+                ww[k] = __shfl_sync(kFull, ew, j & 31);
+                const bool ok = j < cn;
+                const uint32_t *row = m.dist + (uint64_t)vv[k] * kMaxBatch;
+                clo[k] = (ok && lo_on) ? row[lane] : 0;
+                chi[k] = (ok && any_hi && hi_on) ? row[lane + 32] : 0;
             }
-            if (any_hi && hi_on) {
-                const uint32_t nd = d_hi + w;
-                if (nd < row[lane + 32]) imp_hi = nd < atomicMin(&row[lane + 32], nd);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (j0 + k >= cn) break;
+                const uint32_t v = vv[k], w = ww[k];
+                uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+                bool imp_lo = false, imp_hi = false;
+                if (lo_on) {
+                    const uint32_t nd = d_lo + w;
+                    if (nd < clo[k]) imp_lo = nd < atomicMin(&row[lane], nd);
+                }
+                if (any_hi && hi_on) {
+                    const uint32_t nd = d_hi + w;
+                    if (nd < chi[k]) imp_hi = nd < atomicMin(&row[lane + 32], nd);
+                }
+                const unsigned blo = __ballot_sync(kFull, imp_lo), bhi = __ballot_sync(kFull, imp_hi);
+                if ((blo | bhi) && lane == 0)
+                    mark_touched(m, atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull, v);
             }
-            const unsigned blo = __ballot_sync(kFull, imp_lo), bhi = __ballot_sync(kFull, imp_hi);
-            if ((blo | bhi) && lane == 0)
-                mark_touched(m, atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull, v);
         }
     }
 }
@@ -2141,6 +2223,7 @@ asc_status batch_launch(BatchEngine *b) {
     b->it++;
     if (b->sssp) ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
     else if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
+    else if (g->ebits < 32) ms_bfs_expand_kernel<kBitsLayout><<<grid, kBlock, 0, s>>>(m);
     else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);
     if (b->sssp) ms_apply_kernel<false><<<fill_grid(ws, nwords), kBlock, 0, s>>>(m, b->d_plane, b->d_lvl_off, b->it,
                                                                                alive, nwords);
@@ -2234,7 +2317,7 @@ asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint3
         st->iterations = (int32_t)(b->it - it0);
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         float ms = 0;
@@ -2315,7 +2398,7 @@ __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t ti
                     else hi = mid;
                 }
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
-                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : __ldg(a.edges + idx) >> a.wbits;
+                v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : edge_word(a.edges, idx, a.ebits) >> a.wbits;
                 ck[k] = sm.c[lo];
             }
         }
@@ -2343,7 +2426,8 @@ __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
-            v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : __ldg(a.edges + b + j) >> a.wbits) : 0xffffffffu;
+            v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : edge_word(a.edges, b + j, a.ebits) >> a.wbits)
+                         : 0xffffffffu;
         }
 #pragma unroll
         for (int k = 0; k < kUnroll; k++)
@@ -2538,7 +2622,7 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
         st->iterations = it;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = hs[1] * 4ull * g->edge_words;
+        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         st->reached_vertices = V;
@@ -2787,6 +2871,7 @@ extern "C" asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint3
     memset(&a, 0, sizeof(a));
     a.ptr = d_row_offsets;
     a.edges = d_col;
+    a.ebits = 32;
     a.val = d_levels;
     a.visited = visited;
     a.huge_bits = huge_bits;
@@ -2860,9 +2945,9 @@ std::string tune_key(asc_graph *g, asc_algo algo) {
     for (auto &c : name)
         if (c == ' ') c = '_';
     char buf[256];
-    snprintf(buf, sizeof(buf), "%s:V%llu:E%llu:S%llu:W%u:C%u:A%d", name.c_str(), (unsigned long long)g->V,
-             (unsigned long long)g->E, (unsigned long long)g->static_edges, g->edge_words, g->is_csc ? 1 : 0,
-             (int)algo);
+    snprintf(buf, sizeof(buf), "%s:V%llu:E%llu:S%llu:W%u:B%u:C%u:A%d", name.c_str(), (unsigned long long)g->V,
+             (unsigned long long)g->E, (unsigned long long)g->static_edges, g->edge_words, g->ebits,
+             g->is_csc ? 1 : 0, (int)algo);
     return buf;
 }
 

@@ -197,8 +197,9 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     asc_budget_default(&def);
     if (!b) b = &def;
     const uint64_t E = g->E, V = g->V;
-    const uint64_t eb = 4ull * g->edge_words;       // device bytes per edge
-    const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : (double)eb;  // budget unit
+    // device bytes per edge (a bit stream of ebits per edge when narrower than 32)
+    const double eb = g->edge_words == 2 ? 8.0 : g->ebits / 8.0;
+    const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : eb;  // budget unit
     uint64_t frag = b->fragment_edges ? b->fragment_edges : 4096;
     uint64_t st = E;
     bool round_down = false;
@@ -209,12 +210,12 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
         case ASC_BUDGET_FRAC:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget fraction %g is negative", b->value);
             // the fraction of the source edge-array bytes, spent on device-format edges
-            if (b->value * fb >= (double)eb) st = E;
-            else { st = (uint64_t)(b->value * (double)E * fb / (double)eb); round_down = true; }
+            if (b->value * fb >= eb) st = E;
+            else { st = (uint64_t)(b->value * (double)E * fb / eb); round_down = true; }
             break;
         case ASC_BUDGET_BYTES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget bytes %g is negative", b->value);
-            st = (uint64_t)(b->value / (double)eb);
+            st = (uint64_t)(b->value / eb);
             if (st >= E) st = E;
             else round_down = true;
             break;
@@ -224,7 +225,7 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
             size_t freeb = 0, totalb = 0;
             ASC_CUDA(cudaMemGetInfo(&freeb, &totalb));
             uint64_t reduce = (uint64_t)param_size * 4ull * V;
-            uint64_t total_edges = freeb > reduce ? (freeb - reduce) / eb : 0;
+            uint64_t total_edges = freeb > reduce ? (uint64_t)((double)(freeb - reduce) / eb) : 0;
             double k;
             if (b->value > 0) k = b->value;
             else {
@@ -241,6 +242,9 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
         case ASC_BUDGET_EDGES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget edges %g is negative", b->value);
             st = std::min<uint64_t>(E, (uint64_t)b->value);
+            break;
+        case ASC_BUDGET_MANAGED:
+            st = 0;
             break;
         default:
             return fail(ASC_ERR_INVALID, "unknown budget mode %u", b->mode);
@@ -265,7 +269,7 @@ static asc_status upload(asc_graph *g) {
     ASC_CUDA(cudaMalloc(&g->d_ptr, sizeof(uint32_t) * (g->V + 1)));
     ASC_CUDA(cudaMemcpy(g->d_ptr, g->h_ptr, sizeof(uint32_t) * (g->V + 1), cudaMemcpyHostToDevice));
     g->device_vertex_bytes = sizeof(uint32_t) * (g->V + 1);
-    uint64_t sb = 4ull * g->edge_words * g->static_edges;
+    uint64_t sb = g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0;
     ASC_CUDA(cudaMalloc(&g->d_static, sb ? sb : 16));
     if (sb) ASC_CUDA(cudaMemcpy(g->d_static, g->h_edges, sb, cudaMemcpyHostToDevice));
     if (g->is_csc) {
@@ -302,11 +306,79 @@ static asc_status pack_weighted(asc_graph *g) {
     return ASC_OK;
 }
 
+// ASC_BUDGET_MANAGED: the kernels read the edges through a managed copy
+// advised read-mostly, so the driver moves (duplicates) pages to the GPU on
+// first touch, as the reference's UVM baseline does (bfs.cu:263-268).
+static asc_status make_managed(asc_graph *g) {
+    const size_t bytes = sizeof(uint32_t) * (g->E ? edge_store_words(g, g->E) : 1);
+    ASC_CUDA(cudaMallocManaged(&g->managed_edges, bytes));
+    if (g->E) memcpy(g->managed_edges, g->h_edges, bytes);
+    cudaMemLocation loc;
+    loc.type = cudaMemLocationTypeDevice;
+    loc.id = g->device;
+    ASC_CUDA(cudaMemAdvise(g->managed_edges, bytes, cudaMemAdviseSetReadMostly, loc));
+    g->d_host_edges = g->managed_edges;
+    return ASC_OK;
+}
+
+// Edge words that need fewer than 32 bits (the largest destination, or the
+// largest packed destination/weight word, below 2^ebits) are stored as a bit
+// stream of ebits per edge, edge i at bits [i*ebits, (i+1)*ebits): the static
+// region then holds 32/ebits times the edges per byte and the on-demand edges
+// cross the host link in ebits/32 of the bytes; values are unchanged. Kept at
+// 32 bits when packing would save under 1/8 of the bytes, for two-word edges,
+// and when the environment sets ASC_EDGE_PACKING=0.
+static asc_status narrow_edges(asc_graph *g) {
+    if (g->edge_words != 1 || !g->E) return ASC_OK;
+    const char *env = getenv("ASC_EDGE_PACKING");
+    if (env && env[0] == '0') return ASC_OK;
+    const uint32_t *src = g->h_edges;
+    const unsigned nt = host_threads(g->E);
+    std::vector<uint32_t> part(nt, 0);
+    parallel_for(g->E, nt, [&](unsigned t, uint64_t b, uint64_t e) {
+        uint32_t m = 0;
+        for (uint64_t i = b; i < e; i++) m = std::max(m, src[i]);
+        part[t] = m;
+    });
+    uint32_t maxw = 0;
+    for (uint32_t m : part) maxw = std::max(maxw, m);
+    uint32_t bits = 1;
+    while (bits < 32 && (1ull << bits) <= maxw) bits++;
+    if (bits > 28) return ASC_OK;
+    g->ebits = bits;
+    const uint64_t words = edge_store_words(g, g->E);
+    uint32_t *packed = nullptr;
+    ASC_TRY(pinned_alloc((void **)&packed, sizeof(uint32_t) * words));
+    // 32 consecutive edges fill exactly `bits` words, so 32-edge groups pack independently
+    const uint64_t groups = (g->E + 31) / 32;
+    parallel_for(groups, host_threads(groups * 32), [&](unsigned, uint64_t b, uint64_t e) {
+        for (uint64_t grp = b; grp < e; grp++) {
+            uint32_t *out = packed + grp * bits;
+            for (uint32_t k = 0; k < bits; k++) out[k] = 0;
+            const uint64_t i0 = grp * 32, n = std::min<uint64_t>(32, g->E - i0);
+            for (uint32_t j = 0; j < n; j++) {
+                const uint32_t v = src[i0 + j], pos = j * bits, w = pos >> 5, sh = pos & 31;
+                out[w] |= v << sh;
+                if (sh + bits > 32) out[w + 1] |= v >> (32 - sh);
+            }
+        }
+    });
+    packed[words - 1] = 0;
+    cudaFreeHost(g->h_edges);
+    g->h_edges = packed;
+    void *dp = nullptr;
+    ASC_CUDA(cudaHostGetDevicePointer(&dp, g->h_edges, 0));
+    g->d_host_edges = (const uint32_t *)dp;
+    return ASC_OK;
+}
+
 static asc_status finish_graph(asc_graph *g, const asc_budget *budget, asc_graph **out) {
     ASC_TRY(validate_and_measure(g));
     g->file_edge_bytes = 4 * g->edge_words;
     ASC_TRY(pack_weighted(g));
+    ASC_TRY(narrow_edges(g));
     ASC_TRY(compute_static_split(g, budget, g->is_csc ? 17 : (g->file_edge_bytes == 8 ? 15 : 13)));
+    if (budget && budget->mode == ASC_BUDGET_MANAGED) ASC_TRY(make_managed(g));
     ASC_TRY(upload(g));
     *out = g;
     return ASC_OK;
@@ -318,6 +390,7 @@ static void destroy(asc_graph *g) {
     if (g->d_ptr) cudaFree(g->d_ptr);
     if (g->d_static) cudaFree(g->d_static);
     if (g->d_outdeg) cudaFree(g->d_outdeg);
+    if (g->managed_edges) cudaFree(g->managed_edges);
     if (g->h_ptr) cudaFreeHost(g->h_ptr);
     if (g->h_edges) cudaFreeHost(g->h_edges);
     if (g->h_outdeg) cudaFreeHost(g->h_outdeg);
@@ -704,12 +777,13 @@ asc_status asc_graph_info_get(const asc_graph *g, asc_graph_info *info) {
     info->is_csc = g->is_csc;
     info->static_edges = g->static_edges;
     info->static_vertices = g->static_vertices;
-    info->device_edge_bytes = 4ull * g->edge_words * g->static_edges;
+    info->device_edge_bytes = g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0;
     info->device_vertex_bytes = g->device_vertex_bytes + (g->ws ? g->ws->device_bytes : 0);
-    info->host_pinned_bytes = 4ull * g->edge_words * g->E;
+    info->host_pinned_bytes = 4ull * edge_store_words(g, g->E);
     info->max_degree = g->max_degree;
     info->max_weight = g->max_weight;
     info->weight_bits = g->wbits;
+    info->edge_bits = g->edge_words == 2 ? 64 : g->ebits;
     return ASC_OK;
 }
 

@@ -73,6 +73,7 @@ struct asc_server {
     uint64_t used_bytes = 0;
     bool stop = false;
     bool started = false;
+    int single_graph = -1;          // graph the single worker is running, -1 when idle
     std::thread batch_worker, single_worker;
     std::vector<double> lat_ms;
     uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, batches = 0, batch_sources = 0;
@@ -128,6 +129,23 @@ void evict_idle_locked(asc_server *s) {
                 gs.planes = 0;
             }
         }
+}
+
+// Frees what no query is using: idle batch engines with nobody waiting and
+// the single-query state of graphs the single worker is not running (keep is
+// a graph whose state the caller is about to use). Returns the bytes freed.
+uint64_t reclaim_locked(asc_server *s, int keep) {
+    const uint64_t before = s->used_bytes;
+    evict_idle_locked(s);
+    for (uint32_t gi = 0; gi < s->graphs.size(); gi++) {
+        GraphSlot &gs = s->graphs[gi];
+        if ((int)gi == keep || (int)gi == s->single_graph || !gs.ws_bytes || !gs.g->ws) continue;
+        asc::free_workspace(gs.g);
+        s->used_bytes -= gs.ws_bytes;
+        gs.ws_bytes = 0;
+        gs.ws_pr = false;
+    }
+    return before - s->used_bytes;
 }
 
 bool batchable(const asc_server *s, const Query *q) {
@@ -207,6 +225,27 @@ void batch_loop(asc_server *s) {
         admit_locked(s, work);
         if (work.empty()) {
             if (s->stop) return;
+            bool stalled = false;
+            for (const auto &gs : s->graphs) stalled = stalled || !gs.pend[0].empty() || !gs.pend[1].empty();
+            if (stalled) {
+                // queries wait for batch memory while no batch runs: free what
+                // is idle, else wait for the single worker's run, else run the
+                // waiting queries one at a time
+                if (reclaim_locked(s, -1) > 0) continue;
+                if (s->single_graph >= 0) {
+                    s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
+                    continue;
+                }
+                for (auto &gs : s->graphs)
+                    for (int k = 0; k < 2; k++)
+                        while (!gs.pend[k].empty()) {
+                            s->single.push_back(gs.pend[k].front());
+                            gs.pend[k].pop_front();
+                        }
+                evict_idle_locked(s);
+                s->cv_work.notify_all();
+                continue;
+            }
             s->cv_done.notify_all();
             s->cv_work.wait(lk);
             continue;
@@ -283,7 +322,8 @@ void single_loop(asc_server *s) {
                     s->cv_done.notify_all();
                     continue;
                 }
-                evict_idle_locked(s);
+                reclaim_locked(s, (int)q->graph);
+                s->cv_work.notify_all();
                 if (need - have > budget_left(s)) {
                     if (batch_held(s) == 0) {
                         finish(s, q, ASC_ERR_BUDGET);
@@ -319,6 +359,7 @@ void single_loop(asc_server *s) {
             x->state = Q_RUNNING;
             x->t_start = Clock::now();
         }
+        s->single_graph = (int)q->graph;
         lk.unlock();
         asc_stats st;
         asc_status rc = asc_run(gs.g, q->algo, q->source, &q->params, q->out, &st);
@@ -330,6 +371,8 @@ void single_loop(asc_server *s) {
                 if (group[i]->out && q->out) memcpy(group[i]->out, q->out, bytes);
         }
         lk.lock();
+        s->single_graph = -1;
+        s->cv_work.notify_all();
         for (Query *x : group) {
             x->iterations = st.iterations;
             x->batch = (uint32_t)group.size();

@@ -63,6 +63,8 @@ def parse():
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
+    ap.add_argument("--uvm-study", action="store_true",
+                    help="compare BFS on the managed-memory (UVM) engine with the split engine")
     return ap.parse_args()
 
 
@@ -301,10 +303,48 @@ def workload_config(args):
             "l2": "inputs larger than L2 (edge array %.2f GB)" % (4.0 * (1 << args.scale) * args.edge_factor / 1e9)}
 
 
+def uvm_study(args):
+    """The reference's UVM baseline (edges in managed memory, read-mostly, no
+    static region) against the split engine at the same graph and sources:
+    the managed engine's first BFS pays the page migrations, later ones read
+    the GPU-side copies, which sit outside any device budget."""
+    import ascetic_gb300 as A
+    A.lib()
+    ptr, col = A.rmat_csr(args.scale, args.edge_factor, args.seed)
+    srcs = pick_sources(ptr, 8, args.seed)
+    E = int(ptr[-1])
+    out = {"study": "managed-memory (UVM) engine vs split engine", "rmat_scale": args.scale, "edges": E,
+           "sources": len(srcs)}
+    prm = A.make_params(flags=A.RUN_NO_OUTPUT)
+
+    def leg(budget):
+        free0 = A.device_free_bytes()
+        with A.Graph.from_csr(ptr, col, budget=budget) as g:
+            t = time.perf_counter()
+            _, st = g.run("bfs", srcs[0], params=prm)
+            first_ms = (time.perf_counter() - t) * 1e3
+            ms, edges = [], 0
+            for s in srcs:
+                _, st = g.run("bfs", s, params=prm)
+                ms.append(st["ms_total"])
+                edges += st["reached_edges"]
+            used = free0 - A.device_free_bytes()
+            return {"first_run_ms": round(first_ms, 2), "warm_ms_mean": round(sum(ms) / len(ms), 3),
+                    "warm_gteps": round(edges / (sum(ms) * 1e-3) / 1e9, 2),
+                    "device_bytes_in_use": int(used), "static_edges": int(g.info.static_edges)}
+
+    out["managed"] = leg(A.make_budget(managed=True))
+    out["split_budget_%g" % args.budget] = leg(A.make_budget(frac=args.budget))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.pr_study:
         pr_study(args)
+        return
+    if args.uvm_study:
+        uvm_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)
@@ -371,11 +411,12 @@ def main():
         vs += st["frontier_vertices"] - st["ondemand_vertices"]
     peaks = load_peaks()
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
-    # algorithmic bytes: 8 B per edge (column index + destination value) and
-    # 16 B per frontier vertex (two offsets, own value, list entry)
-    alg_s = 8.0 * ed_s + 16.0 * vs
+    # algorithmic bytes: the stored column (edge_bits / 8 B) + 4 B destination
+    # value per edge and 16 B per frontier vertex (two offsets, own value, list entry)
+    eb = info.edge_bits / 8.0
+    alg_s = (eb + 4.0) * ed_s + 16.0 * vs
     hbm_gbs = alg_s / (ms_s * 1e-3) / 1e9 if ms_s else 0.0
-    link_bytes = 4.0 * ed_o
+    link_bytes = eb * ed_o
     dma_gbs, smread_gbs = A.link_probe(1 << 30, 3)
     link_gbs = link_bytes / (ms_o * 1e-3) / 1e9 if ms_o else 0.0
     traffic = load_traffic()
@@ -405,7 +446,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic RMAT (seeded)",
             "config": workload_config(args), "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "roofline": roofline, "roofline_static_hbm": roof_static, "roofline_ondemand_link": roof_link,
-            "graph": {"V": V, "E": int(g.E), "static_edges": int(info.static_edges),
+            "graph": {"V": V, "E": int(g.E), "edge_bits": int(info.edge_bits), "static_edges": int(info.static_edges),
                       "static_vertices": int(info.static_vertices), "device_edge_bytes": int(info.device_edge_bytes),
                       "ondemand_bytes_per_bfs": int(od_bytes / args.steps), "iterations_per_bfs": iters / args.steps,
                       "generate_s": round(t_gen, 2)},

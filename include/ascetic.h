@@ -69,7 +69,11 @@ typedef enum asc_budget_mode {
     ASC_BUDGET_BYTES = 2,    /* value = bytes for the static region */
     ASC_BUDGET_ADVISE_K = 3, /* value = reference --adviseK: fraction of free device memory left
                                 after the vertex arrays (GraphMeta.cuh:310-354); 0 = its auto formula */
-    ASC_BUDGET_EDGES = 4     /* value = exact static edge count (no fragment rounding) */
+    ASC_BUDGET_EDGES = 4,    /* value = exact static edge count (no fragment rounding) */
+    ASC_BUDGET_MANAGED = 5   /* comparison engine, the reference's UVM baseline (bfs.cu:249-273): no
+                                static region; the edge array lives in CUDA managed memory advised
+                                read-mostly and the driver copies pages to the GPU as kernels touch
+                                them. Device use is then up to the driver, outside any cap. */
 } asc_budget_mode;
 
 typedef struct asc_budget {
@@ -84,7 +88,8 @@ typedef struct asc_graph asc_graph;
 typedef struct asc_graph_info {
     uint64_t vertices;
     uint64_t edges;
-    uint32_t edge_bytes;          /* device/host bytes per edge: 4 (destination or packed) or 8 ({dst, weight}) */
+    uint32_t edge_bytes;          /* bytes per edge of the source layout: 4 (destination or packed) or 8
+                                     ({dst, weight}); edge_bits gives the stored width */
     uint32_t is_csc;              /* 1 for .bcsc (in-edges + out-degree block) */
     uint64_t static_edges;        /* edges in the device-resident prefix */
     uint64_t static_vertices;     /* vertices [0, static_vertices) have every edge in the prefix */
@@ -96,7 +101,11 @@ typedef struct asc_graph_info {
     uint32_t weight_bits;         /* > 0: weighted edges stored packed as (dst << bits) | weight in 4 bytes
                                      (whenever destinations and weights fit): half the bytes per edge,
                                      twice the edges in the same static-region bytes */
-    uint32_t reserved;
+    uint32_t edge_bits;           /* stored bits per edge: 64 ({dst, weight}), 32, or fewer when every
+                                     edge word fits (a bit stream of edge_bits per edge, in HBM and in
+                                     pinned host memory: more static edges per budget byte, fewer
+                                     bytes over the host link; ASC_EDGE_PACKING=0 in the environment
+                                     keeps 32) */
 } asc_graph_info;
 
 typedef enum asc_pr_mode {
@@ -153,6 +162,8 @@ size_t asc_last_error(char *buf, size_t n);
 const char *asc_version(void);
 /* Number of usable CUDA devices (0 when none); never fails. */
 int asc_device_count(void);
+/* Free and total bytes of the current CUDA device (cudaMemGetInfo). */
+asc_status asc_device_memory(uint64_t *free_bytes, uint64_t *total_bytes);
 
 /* ---- graphs -------------------------------------------------------------- */
 void asc_budget_default(asc_budget *b);

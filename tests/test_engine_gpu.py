@@ -77,7 +77,7 @@ def test_bfs_matches_oracle(frac):
                 got, st = g.run("bfs", s, params=A.make_params(flags=flags))
                 assert np.array_equal(got, exp), (frac, s, flags)
                 assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
-                if 0 < frac < 1 and st["reached_vertices"] > 1000:
+                if g.info.static_edges < g.E and st["reached_vertices"] > 1000:
                     assert st["ondemand_edges"] > 0
                 iters.add(st["iterations"])
             # BFS runs one level per iteration whatever drives the loop
@@ -328,3 +328,94 @@ def test_ptgraph_cli_matches_oracle():
             assert np.array_equal(got, exp), algo
     r = subprocess.run([A.PTGRAPH_PATH, "--input", os.path.join(d, "missing.bcsr")], capture_output=True, text=True)
     assert r.returncode == 2 and "bad graph file" in r.stderr
+
+
+def test_managed_comparison_engine():
+    """The UVM comparison engine (edges in managed memory, no static region)
+    computes the same values as the split engine."""
+    ptr, adj = A.rmat_csr(13, 16, 41, weights=(1, 63))
+    col = adj[:, 0].copy()
+    cptr, ccol, od = A.formats.transpose(ptr, col)
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(managed=True)) as g:
+        assert g.info.static_edges == 0
+        for s in (0, 77):
+            for _ in range(2):  # first touch migrates pages; the second run reads them on the GPU
+                got, _ = g.run("bfs", s)
+                assert np.array_equal(got, oracle.bfs(ptr, col, s))
+            got, _ = g.run("sssp", s)
+            assert np.array_equal(got, oracle.sssp(ptr, adj, s))
+        got, _ = g.run_batch("bfs", [0, 77])
+        assert np.array_equal(got[1], oracle.bfs(ptr, col, 77))
+    with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(managed=True)) as g:
+        got, _ = g.run("pr")
+        assert np.abs(got - oracle.pr_ref(cptr, ccol, od)[0]).max() <= PR_TOL
+
+
+def test_converted_edge_list_runs(tmp_path):
+    """asc-convert output opens in every layout and runs like the oracle on
+    the edge list (CSR / CSC built by the oracle's converter restatement)."""
+    import subprocess
+    rng = np.random.default_rng(7)
+    n, V = 20000, 3000
+    src, dst = rng.integers(0, V, n), rng.integers(0, V, n)
+    path = tmp_path / "g.txt"
+    path.write_text("# edge list\n" + "\n".join("%d %d" % e for e in zip(src, dst)) + "\n")
+    r = subprocess.run([A.CONVERT_PATH, str(path), "--to", "bcsr,bwcsr,bcsc,bcsr32"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    Vc, ptr, order, outdeg = oracle.converter(src, dst)
+    col = dst.astype(np.uint32)[order]
+    w = oracle.converter_ref_weights(n)[order]
+    adj = np.stack([col, w], axis=1)
+    _, cptr, corder, _ = oracle.converter(src, dst, by_dst=True)
+    ccol = src.astype(np.uint32)[corder]
+    stem = str(tmp_path / "g")
+    for ext in ("bcsr", "bcsr32"):
+        with A.Graph.open(stem + "." + ext, budget=A.make_budget(frac=0.3)) as g:
+            got, _ = g.run("bfs", int(src[0]))
+            assert np.array_equal(got, oracle.bfs(ptr, col, int(src[0])))
+    with A.Graph.open(stem + ".bwcsr", budget=A.make_budget(frac=0.3)) as g:
+        got, _ = g.run("sssp", int(src[0]))
+        assert np.array_equal(got, oracle.sssp(ptr, adj, int(src[0])))
+    with A.Graph.open(stem + ".bcsc", budget=A.make_budget(frac=0.3)) as g:
+        got, _ = g.run("pr")
+        assert np.abs(got - oracle.pr_ref(cptr, ccol, outdeg)[0]).max() <= PR_TOL
+
+
+@pytest.mark.parametrize("frac", [0.25, 0.0, 1.0])
+def test_bit_packed_edges_match_32_bit_edges(frac, monkeypatch):
+    """Unweighted edges are stored as a bit stream of bits(max id) per edge
+    (more static edges per budget byte, fewer link bytes); results equal the
+    32-bit layout's and the oracle's."""
+    ptr, col = A.rmat_csr(14, 16, 61)
+    cptr, ccol, od = A.formats.transpose(ptr, col)
+    sptr, scol = A.formats.symmetrize(ptr, col)
+    runs = {}
+    for packing in ("1", "0"):
+        monkeypatch.setenv("ASC_EDGE_PACKING", packing)
+        with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+            info = g.info
+            assert info.edge_bits == (14 if packing == "1" else 32)
+            out = {"static": info.static_edges}
+            for s in (0, 1234):
+                out["bfs", s] = g.run("bfs", s)[0]
+            out["batch"] = g.run_batch("bfs", [0, 1234, 77])[0]
+            out["pr_push"] = g.run("pr")[0]
+        with A.Graph.from_csr(sptr, scol, budget=A.make_budget(frac=frac)) as g:
+            out["cc"] = g.run("cc")[0]
+        with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=frac)) as g:
+            out["pr"] = g.run("pr")[0]
+            out["pr_std"] = g.run("pr", params=A.make_params(pr_mode=A.PR_STD, precision=A.F32))[0]
+        runs[packing] = out
+    p, u = runs["1"], runs["0"]
+    if 0 < frac < 1:
+        # the same budget bytes hold 32/14 times the edges (down to whole fragments)
+        assert p["static"] > 2 * u["static"]
+    for s in (0, 1234):
+        exp = oracle.bfs(ptr, col, s)
+        assert np.array_equal(p["bfs", s], exp) and np.array_equal(u["bfs", s], exp)
+    assert np.array_equal(p["batch"][1], oracle.bfs(ptr, col, 1234))
+    assert np.array_equal(p["cc"], oracle.cc(sptr, scol)) and np.array_equal(u["cc"], p["cc"])
+    ref = oracle.pr_ref(cptr, ccol, od)[0]
+    assert np.abs(p["pr"] - ref).max() <= PR_TOL and np.abs(p["pr_push"] - ref).max() <= PR_TOL
+    std = oracle.pr_std(cptr, ccol, od)[0]
+    assert np.abs(p["pr_std"].astype(np.float64) - std).max() <= PR_TOL

@@ -108,3 +108,42 @@ def test_budget_and_cancel():
             outs = [srv.wait(t) for t in ts]
             st = srv.stats()
             assert st["completed"] + st["cancelled"] == 20
+
+
+@pytest.mark.parametrize("extra", [1_000_000, 2_500_000, 5_000_000, 10_000_000])
+def test_tight_shared_budget_completes(extra):
+    """Several graphs under a budget too small for all their batch engines at
+    once, every query submitted at t=0: engines take turns (idle ones and unused
+    single-query state are freed for waiting queries, and queries that cannot
+    get batch memory run whole), every query completes with the solo values."""
+    data = [A.rmat_csr(13, 16, 51, weights=(1, 63)), A.rmat_csr(12, 16, 52, weights=(1, 63)),
+            A.rmat_csr(11, 16, 53, weights=(1, 63))]
+    graphs = [A.Graph.from_csr(p, adj, budget=A.make_budget(frac=0.25)) for p, adj in data]
+    base = sum(g.info.device_edge_bytes + 4 * (g.V + 1) for g in graphs)
+    rng = np.random.default_rng(extra)
+    std32 = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
+    plan = []
+    for i in range(120):
+        gi = int(rng.integers(0, 3))
+        r = rng.random()
+        algo = "bfs" if r < 0.5 else "sssp" if r < 0.8 else "cc" if r < 0.9 else "pr"
+        src = int(rng.integers(0, graphs[gi].V)) if algo in ("bfs", "sssp") else 0
+        plan.append((gi, algo, src))
+    with A.Server(budget_bytes=base + extra) as srv:
+        ids = [srv.add_graph(g) for g in graphs]
+        tickets = [srv.submit(ids[gi], algo, src, params=std32 if algo == "pr" else None)
+                   for gi, algo, src in plan]
+        results = [srv.wait(t, timeout_ms=120000) for t in tickets]
+        st = srv.stats()
+        assert st["device_bytes"] <= base + extra
+    assert st["completed"] == len(plan) and st["failed"] == 0
+    for (gi, algo, src), (out, info) in zip(plan, results):
+        ptr, adj = data[gi]
+        if algo == "bfs":
+            assert np.array_equal(out, oracle.bfs(ptr, adj[:, 0], src))
+        elif algo == "sssp":
+            assert np.array_equal(out, oracle.sssp(ptr, adj, src))
+        elif algo == "cc":
+            assert np.array_equal(out, oracle.cc(ptr, adj[:, 0]))
+    for g in graphs:
+        g.close()
