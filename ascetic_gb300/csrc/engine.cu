@@ -43,9 +43,12 @@ namespace asc {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-// Minimum resident CTAs per SM asked of the expansion kernels (register cap).
+// Minimum resident CTAs per SM asked of the expansion kernels (register cap):
+// 8 x 256 threads fill an SM, 32 registers each. Measured on RMAT scale 24 with
+// bit-packed edges: 65.6 GTEPS at 8, 64.5 at 6, 57.3 at 4 (64 registers, half
+// the warps: the loads over the host link want every warp the SM can hold).
 #ifndef ASC_EXPAND_MIN_BLOCKS
-#define ASC_EXPAND_MIN_BLOCKS 4
+#define ASC_EXPAND_MIN_BLOCKS 8
 #endif
 constexpr int kWarps = kBlock / 32;
 
@@ -289,8 +292,7 @@ __device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem 
     sm.vu[threadIdx.x] = vu;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(act);
-    // software pipeline: the column loads of the next pass are in flight while
-    // this pass probes and updates its destinations
+    // each pass issues kUnroll column loads per thread before any update
     auto load_pass = [&](uint32_t base, uint32_t (&v)[kUnroll], uint32_t (&nv)[kUnroll]) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
@@ -308,20 +310,13 @@ __device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem 
             }
         }
     };
-    uint32_t v[kUnroll], nv[kUnroll];
-    if (total) load_pass(0, v, nv);
     for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
-        uint32_t vn[kUnroll], nvn[kUnroll], cur[kUnroll];
-        if (base + kUnroll * kBlock < total) load_pass(base + kUnroll * kBlock, vn, nvn);
+        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+        load_pass(base, v, nv);
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
-#pragma unroll
-        for (int k = 0; k < kUnroll; k++) {
-            v[k] = vn[k];
-            nv[k] = nvn[k];
-        }
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -378,20 +373,13 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
             if (j < n) load_edge<ALG, WORDS>(a, vu, b + j, v[k], nv[k]);
         }
     };
-    uint32_t v[kUnroll], nv[kUnroll];
-    if (n) load_pass(0, v, nv);
     for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
-        uint32_t vn[kUnroll], nvn[kUnroll], cur[kUnroll];
-        if (base + kUnroll * kBlock < n) load_pass(base + kUnroll * kBlock, vn, nvn);
+        uint32_t v[kUnroll], nv[kUnroll], cur[kUnroll];
+        load_pass(base, v, nv);
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) cur[k] = nv[k] != 0xffffffffu ? probe<ALG>(a, v[k]) : 0;
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) count_next(a, lower<ALG>(a, v[k], nv[k], cur[k]), v[k], s_next);
-#pragma unroll
-        for (int k = 0; k < kUnroll; k++) {
-            v[k] = vn[k];
-            nv[k] = nvn[k];
-        }
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
