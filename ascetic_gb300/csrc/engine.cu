@@ -268,7 +268,12 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
 // Each thread handles kUnroll edges per pass: all column loads are issued
 // first, then all destination-value loads, then the updates, so a thread keeps
 // kUnroll independent reads in flight (on-demand column reads cross the host link).
-constexpr int kUnroll = 4;
+// (measured with bit-packed edges at 8 CTAs per SM: 4 -> 65.7 GTEPS, 6 -> 64.3,
+// 8 -> 62.2; more loads per thread spill at 32 registers)
+#ifndef ASC_EXPAND_UNROLL
+#define ASC_EXPAND_UNROLL 4
+#endif
+constexpr int kUnroll = ASC_EXPAND_UNROLL;
 
 // Expands up to kBlock frontier vertices, one per thread (act = false where a
 // thread has none): a block scan of their degrees lays the edges out as one

@@ -280,16 +280,17 @@ static asc_status upload(asc_graph *g) {
     return ASC_OK;
 }
 
-// Weighted edges are packed into one u32, (dst << wbits) | weight, when the
-// destination needs at most 32 - wbits bits and every weight fits in wbits:
+// Weighted edges are packed into one u32, (dst << wbits) | weight, wbits the
+// bits of the largest weight, when destination and weight bits fit in 32:
 // half the bytes per edge over the host link and twice the edges in the same
 // static-region bytes; values are unchanged. The AoS host copy is released.
 static asc_status pack_weighted(asc_graph *g) {
     if (g->edge_words != 2) return ASC_OK;
     uint32_t vbits = 1;
     while (vbits < 32 && (1ull << vbits) < g->V) vbits++;
-    const uint32_t wbits = 32 - vbits;
-    if (wbits == 0 || (uint64_t)g->max_weight >= (1ull << wbits)) return ASC_OK;
+    uint32_t wbits = 1;  // as few as the largest weight needs: the high bits stay free for a bit stream
+    while (wbits < 32 && (1ull << wbits) <= (uint64_t)g->max_weight) wbits++;
+    if (vbits + wbits > 32) return ASC_OK;
     uint32_t *packed = nullptr;
     ASC_TRY(pinned_alloc((void **)&packed, sizeof(uint32_t) * (g->E ? g->E : 1)));
     const uint32_t *aos = g->h_edges;
@@ -326,8 +327,8 @@ static asc_status make_managed(asc_graph *g) {
 // stream of ebits per edge, edge i at bits [i*ebits, (i+1)*ebits): the static
 // region then holds 32/ebits times the edges per byte and the on-demand edges
 // cross the host link in ebits/32 of the bytes; values are unchanged. Kept at
-// 32 bits when packing would save under 1/8 of the bytes, for two-word edges,
-// and when the environment sets ASC_EDGE_PACKING=0.
+// 32 bits when it would save under 2 bits per edge, for two-word edges, and
+// when the environment sets ASC_EDGE_PACKING=0.
 static asc_status narrow_edges(asc_graph *g) {
     if (g->edge_words != 1 || !g->E) return ASC_OK;
     const char *env = getenv("ASC_EDGE_PACKING");
@@ -344,7 +345,7 @@ static asc_status narrow_edges(asc_graph *g) {
     for (uint32_t m : part) maxw = std::max(maxw, m);
     uint32_t bits = 1;
     while (bits < 32 && (1ull << bits) <= maxw) bits++;
-    if (bits > 28) return ASC_OK;
+    if (bits > 30) return ASC_OK;
     g->ebits = bits;
     const uint64_t words = edge_store_words(g, g->E);
     uint32_t *packed = nullptr;

@@ -3,8 +3,9 @@
 Workload (the configuration the headline metric is quoted on): RMAT scale 24
 (16,777,216 vertices), edge factor 16 (268,435,456 directed edges), a=.57
 b=.19 c=.19 d=.05, seed 2, self-loops and duplicates kept; static region
-capped at 25% of the edge-array bytes so three quarters of the edges are read
-on demand from pinned host memory. One step = one BFS from one of 8 seeded
+capped at 25% of the edge-array bytes (the engine stores edges as a 24-bit
+stream, so the cap holds a third of them); the rest are read on demand from
+pinned host memory. One step = one BFS from one of 8 seeded
 random sources with out-degree > 0 (rotating). SSSP (weights uniform in
 [1,63], 25% of the 8-byte edge array) and CC (symmetrised graph, 25%) from the
 same configuration are measured after the timed BFS steps and reported beside
@@ -338,6 +339,42 @@ def uvm_study(args):
     print(json.dumps(out), flush=True)
 
 
+def replica_setup():
+    """Multi-GPU runs are replicas (the path does not shard): under torchrun
+    every rank runs the same workload on its own GPU; a gloo group on the host
+    gives the barriers and the cross-rank sums/max. Returns (rank, world)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        local = int(os.environ.get("LOCAL_RANK", str(rank)))
+        visible = [d for d in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if d]
+        # one device per replica process, chosen before the engine library loads
+        os.environ["CUDA_VISIBLE_DEVICES"] = visible[local] if local < len(visible) else str(local)
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+    return rank, world
+
+
+def replica_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_reduce(edges, seconds, world):
+    """Whole-job totals: edges summed over the replicas, time the slowest one."""
+    if world <= 1:
+        return edges, seconds
+    import torch
+    import torch.distributed as dist
+    e = torch.tensor([float(edges)], dtype=torch.float64)
+    t = torch.tensor([float(seconds)], dtype=torch.float64)
+    dist.all_reduce(e, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return e.item(), t.item()
+
+
 def main():
     args = parse()
     if args.pr_study:
@@ -349,6 +386,7 @@ def main():
     if args.impl == "reference":
         reference_arm(args)
         return
+    rank, world = replica_setup()
     import __graft_entry__
     import ascetic_gb300 as A
     if not os.path.exists(A.LIB_PATH):
@@ -371,6 +409,7 @@ def main():
     clocks.start()
     time.sleep(0.3)
     tot_edges, tot_ms, launches, od_bytes, iters = 0, 0.0, 0, 0, 0
+    replica_barrier(world)
     t_wall = time.perf_counter()
     step_flags = A.RUN_NO_OUTPUT | (A.RUN_PHASE_TIMING if args.split else 0)
     for i in range(args.steps):
@@ -381,8 +420,10 @@ def main():
         od_bytes += st["ondemand_bytes"]
         iters += st["iterations"]
     t_wall = time.perf_counter() - t_wall
+    replica_barrier(world)
     clk = clocks.stop()
-    value = tot_edges / (tot_ms * 1e-3) / 1e9
+    job_edges, job_s = replica_reduce(tot_edges, tot_ms * 1e-3, world)
+    value = job_edges / job_s / 1e9
 
     # end to end through the C ABI with a pageable host result buffer
     out = np.empty(V, np.uint32)
@@ -394,6 +435,12 @@ def main():
         e2e_edges += st["reached_edges"]
         e2e_od += st["ondemand_bytes"]
     n_e2e = min(args.steps, 8)
+    e2e_edges, e2e_s = replica_reduce(e2e_edges, e2e_s, world)
+    if rank != 0:
+        # the replicas' share ends here: rank 0 adds the single-GPU legs and prints
+        g.close()
+        replica_barrier(world)
+        return
     e2e = {"value": round(e2e_edges / e2e_s / 1e9, 4), "unit": "GTEPS",
            "h2d_bytes_per_step": int(e2e_od / n_e2e) + 4, "d2h_bytes_per_step": 4 * V,
            "note": "h2d = on-demand edge bytes read over the host link per BFS plus the source id"}
@@ -529,7 +576,10 @@ def main():
         line["cpu_baseline"] = {"value": round(re / dt / 1e9, 4), "unit": "GTEPS", "cores": 1, "kind": "port",
                                 "sample": "one serial queue BFS (oracle orc_bfs) from source %d of the same graph, "
                                           "%.2f s" % (srcs[0], dt)}
+    if world > 1:
+        line["config"]["parallelism"] = "%d independent replicas (the path does not shard)" % world
     print(json.dumps(line), flush=True)
+    replica_barrier(world)
 
 
 if __name__ == "__main__":

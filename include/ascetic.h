@@ -98,14 +98,15 @@ typedef struct asc_graph_info {
     uint64_t host_pinned_bytes;   /* pinned host copy of the edge array (on-demand source) */
     uint32_t max_degree;
     uint32_t max_weight;          /* 0 for unweighted graphs */
-    uint32_t weight_bits;         /* > 0: weighted edges stored packed as (dst << bits) | weight in 4 bytes
-                                     (whenever destinations and weights fit): half the bytes per edge,
-                                     twice the edges in the same static-region bytes */
-    uint32_t edge_bits;           /* stored bits per edge: 64 ({dst, weight}), 32, or fewer when every
-                                     edge word fits (a bit stream of edge_bits per edge, in HBM and in
-                                     pinned host memory: more static edges per budget byte, fewer
-                                     bytes over the host link; ASC_EDGE_PACKING=0 in the environment
-                                     keeps 32) */
+    uint32_t weight_bits;         /* > 0: weighted edges stored packed as (dst << bits) | weight, bits the
+                                     width of the largest weight (whenever destination and weight bits
+                                     fit in 32): half the bytes per edge or less, twice the edges or
+                                     more in the same static-region bytes */
+    uint32_t edge_bits;           /* stored bits per edge: 64 ({dst, weight}), 32, or at most 30 when
+                                     every edge word fits (a bit stream of edge_bits per edge, in HBM
+                                     and in pinned host memory: more static edges per budget byte,
+                                     fewer bytes over the host link; ASC_EDGE_PACKING=0 in the
+                                     environment keeps 32) */
 } asc_graph_info;
 
 typedef enum asc_pr_mode {

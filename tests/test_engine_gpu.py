@@ -132,18 +132,20 @@ def test_batch_sssp_rows_equal_single_source(frac):
 
 
 def test_packed_and_unpacked_weighted_edges():
-    """Weighted edges are stored packed (dst << bits | weight) when they fit,
-    AoS otherwise; both give the oracle's distances, and a byte budget holds
-    twice the edges when packed."""
+    """Weighted edges are stored packed (dst << bits | weight, bits the width of
+    the largest weight: 13 + 6 = 19-bit words here, stored as a bit stream) when
+    they fit, AoS otherwise; both give the oracle's distances, and a byte budget
+    holds 64/19 times the edges when packed."""
     ptr, adj = A.rmat_csr(13, 8, 36, weights=(1, 63))
     big = adj.copy()
     big[:, 1] = (big[:, 1].astype(np.uint64) * 40000).astype(np.uint32)   # needs > 19 weight bits
     for arr, packed in ((adj, True), (big, False)):
         with A.Graph.from_csr(ptr, arr, budget=A.make_budget(frac=0.2)) as g:
-            assert (g.info.weight_bits > 0) == packed
+            assert (g.info.weight_bits == 6) == packed and (g.info.weight_bits > 0) == packed
             assert g.info.edge_bytes == (4 if packed else 8)
+            assert g.info.edge_bits == (19 if packed else 64)
             frac_edges = g.info.static_edges / g.E
-            assert (0.3 < frac_edges < 0.45) if packed else (0.1 < frac_edges < 0.22)
+            assert abs(frac_edges - 0.2 * 64 / g.info.edge_bits) < 0.05, frac_edges
             for s in (0, 41):
                 got, _ = g.run("sssp", s)
                 assert np.array_equal(got, oracle.sssp(ptr, arr, s)), (packed, s)
@@ -419,3 +421,24 @@ def test_bit_packed_edges_match_32_bit_edges(frac, monkeypatch):
     assert np.abs(p["pr"] - ref).max() <= PR_TOL and np.abs(p["pr_push"] - ref).max() <= PR_TOL
     std = oracle.pr_std(cptr, ccol, od)[0]
     assert np.abs(p["pr_std"].astype(np.float64) - std).max() <= PR_TOL
+
+
+@pytest.mark.parametrize("V", [2, 3, 5, 33, 1000, 70000, (1 << 20) + 3])
+def test_bit_stream_widths(V):
+    """Bit streams of every width class (1 bit for ids {0, 1} up to 21 bits),
+    with edges straddling word boundaries, split at several budgets."""
+    rng = np.random.default_rng(V)
+    E = min(40 * V, 400000)
+    src = np.sort(rng.integers(0, V, E))
+    dst = rng.integers(0, V, E)
+    dst[-1] = V - 1  # the widest id is present
+    ptr, col = A.formats.csr_from_edges(V, src, dst)
+    bits = max(1, int(V - 1).bit_length())
+    for frac in (0.0, 0.3, 1.0):
+        with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+            assert g.info.edge_bits == bits
+            for s in (0, V - 1, V // 2):
+                got, _ = g.run("bfs", s)
+                assert np.array_equal(got, oracle.bfs(ptr, col, s)), (V, frac, s)
+            got, _ = g.run("cc")
+            assert np.array_equal(got, oracle.cc(ptr, col)), (V, frac)

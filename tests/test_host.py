@@ -4,6 +4,7 @@ round trips, and the command line exists. No compute call reaches a GPU."""
 import os
 import re
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -133,3 +134,38 @@ def test_malformed_files_are_rejected_before_any_device_work():
     with pytest.raises(A.AscError) as e:
         A.Graph.open(os.path.join(d, "missing.bcsr"))
     assert e.value.status == A.ERR_BAD_FILE
+
+
+def _replica_worker(rank, port, q):
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                       "WORLD_SIZE": "2", "LOCAL_RANK": str(rank), "CUDA_VISIBLE_DEVICES": "4,5"})
+    sys.path.insert(0, ROOT)
+    import bench
+    r, w = bench.replica_setup()
+    bench.replica_barrier(w)
+    edges, secs = bench.replica_reduce(1000 * (rank + 1), 0.5 + rank, w)
+    q.put((r, w, edges, secs, os.environ["CUDA_VISIBLE_DEVICES"]))
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def test_bench_replicas_gloo_world2():
+    """bench.py under torchrun runs one replica per GPU: a gloo group gives the
+    barrier, whole-job edges (sum) and time (slowest replica). Two CPU ranks."""
+    import socket
+    import torch.multiprocessing as mp
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_worker, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[:4] for r in res] == [(0, 2, 3000.0, 1.5), (1, 2, 3000.0, 1.5)]
+    assert [r[4] for r in res] == ["4", "5"]   # one device per replica, by local rank
