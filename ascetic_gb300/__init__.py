@@ -43,7 +43,7 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
             "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
             "asc_server_stats_get", "asc_server_destroy", "asc_graph_get_tuning", "asc_graph_set_tuning",
-            "asc_graph_tune", "asc_device_memory"]
+            "asc_graph_tune", "asc_device_memory", "asc_link_probe_runs"]
 TUNE_NO_CACHE = 1
 SERVE_BATCHED, SERVE_FIFO = 0, 1
 
@@ -163,6 +163,7 @@ def lib():
                            ctypes.c_int),
         "asc_write_graph": ([ctypes.c_char_p, ctypes.c_int, c_u64, c_u64, c_vp, c_vp, c_vp], ctypes.c_int),
         "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
+        "asc_link_probe_runs": ([c_u64, c_u32, ctypes.c_int, P(c_dbl)], ctypes.c_int),
         "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
         "asc_run_batch": ([c_vp, ctypes.c_int, c_vp, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
         "asc_server_config_default": ([P(ServerConfig)], None),
@@ -457,6 +458,13 @@ def link_probe(nbytes=1 << 30, iters=5):
     a, b = ctypes.c_double(), ctypes.c_double()
     _check(lib().asc_link_probe(nbytes, iters, ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def link_probe_runs(run_bytes, nbytes=1 << 30, iters=3):
+    """Host-link GB/s when warps read runs of run_bytes at random offsets."""
+    g = ctypes.c_double()
+    _check(lib().asc_link_probe_runs(nbytes, run_bytes, iters, ctypes.byref(g)))
+    return g.value
 
 
 def write_graph(path, fmt, ptr, edges, outdeg=None):

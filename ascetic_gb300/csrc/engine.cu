@@ -2668,7 +2668,83 @@ __global__ void link_read_kernel(const uint4 *__restrict__ src, size_t n16, unsi
     }
     if (acc == 0x9e3779b9u) atomicAdd(sink, 1ull);  // keeps the loads live
 }
+__device__ __forceinline__ uint64_t probe_mix(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    return x ^ (x >> 33);
+}
+
+// Each warp reads `runs` runs of L consecutive words at pseudo-random word
+// offsets in [0, n4 - L), four runs in flight, lanes striding the run: the
+// access shape of short adjacency lists read over the host link.
+__global__ void link_runs_kernel(const uint32_t *__restrict__ src, uint64_t n4, uint32_t L, uint32_t runs,
+                                 unsigned long long *sink) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t acc = 0;
+    for (uint32_t r = 0; r < runs; r += 4) {
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint64_t off = probe_mix(warp * 1000003ull + r + k) % (n4 - L);  // off + L < n4
+            v[k] = 0;
+            for (uint32_t j = lane; j < L; j += 32) v[k] ^= __ldg(src + off + j);
+        }
+        acc ^= v[0] ^ v[1] ^ v[2] ^ v[3];
+    }
+    if (acc == 0x9e3779b9u) atomicAdd(sink, 1ull);  // keeps the loads live
+}
 }  // namespace
+
+extern "C" asc_status asc_link_probe_runs(uint64_t bytes, uint32_t run_bytes, int iters, double *gbs) {
+    using namespace asc;
+    if (bytes < (1u << 20) || iters < 1 || run_bytes < 4 || run_bytes % 4 || run_bytes > bytes / 16)
+        return fail(ASC_ERR_INVALID, "asc_link_probe_runs: bytes >= 1 MiB, 4 <= run_bytes <= bytes/16, "
+                                     "run_bytes a multiple of 4, iters >= 1");
+    bytes &= ~(uint64_t)15;
+    void *h = nullptr, *hd = nullptr;
+    unsigned long long *sink = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    asc_status st = ASC_OK;
+    double best = 0;
+    int sms = 0, dev = 0;
+    auto chk = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == ASC_OK) st = cuda_fail(e, what, __FILE__, __LINE__);
+        return st == ASC_OK;
+    };
+    if (chk(cudaHostAlloc(&h, bytes, cudaHostAllocMapped | cudaHostAllocPortable), "cudaHostAlloc") &&
+        chk(cudaHostGetDevicePointer(&hd, h, 0), "cudaHostGetDevicePointer") &&
+        chk(cudaMalloc(&sink, 8), "cudaMalloc") && chk(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream") &&
+        chk(cudaEventCreate(&e0), "event") && chk(cudaEventCreate(&e1), "event") && chk(cudaGetDevice(&dev), "dev") &&
+        chk(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr")) {
+        memset(h, 1, bytes);
+        const uint64_t n4 = bytes / 4;
+        const uint32_t L = run_bytes / 4;
+        const uint64_t warps = (uint64_t)sms * 8 * (256 / 32);
+        // about one pass over the buffer, a multiple of 4 runs per warp
+        const uint32_t runs = (uint32_t)std::max<uint64_t>(4, (n4 / (warps * L)) & ~3ull);
+        for (int i = 0; i < iters + 1 && st == ASC_OK; i++) {
+            float ms = 0;
+            chk(cudaEventRecord(e0, s), "rec");
+            link_runs_kernel<<<sms * 8, 256, 0, s>>>((const uint32_t *)hd, n4, L, runs, sink);
+            chk(cudaGetLastError(), "launch");
+            chk(cudaEventRecord(e1, s), "rec");
+            chk(cudaEventSynchronize(e1), "sync");
+            chk(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            if (i > 0 && ms > 0) best = std::max(best, (double)warps * runs * run_bytes / (ms * 1e6));
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (sink) cudaFree(sink);
+    if (h) cudaFreeHost(h);
+    if (gbs) *gbs = best;
+    return st;
+}
 
 extern "C" asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double *sm_read_gbs) {
     using namespace asc;

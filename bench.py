@@ -64,6 +64,8 @@ def parse():
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
+    ap.add_argument("--link-study", action="store_true",
+                    help="host-link rate by run length and the BFS's pattern-limited on-demand ceiling")
     ap.add_argument("--uvm-study", action="store_true",
                     help="compare BFS on the managed-memory (UVM) engine with the split engine")
     return ap.parse_args()
@@ -304,6 +306,68 @@ def workload_config(args):
             "l2": "inputs larger than L2 (edge array %.2f GB)" % (4.0 * (1 << args.scale) * args.edge_factor / 1e9)}
 
 
+def link_study(args):
+    """How fast can the on-demand reads of this BFS go? The host link's rate
+    depends on how long the contiguous runs are (short adjacency lists use
+    32-byte sectors and link requests partly). Measures the rate by run length
+    (asc_link_probe_runs), takes the on-demand run lengths of every BFS
+    iteration from the engine's own levels (consecutive frontier vertices of the
+    on-demand region, zero-degree vertices skipped, stored edge width), and
+    predicts the pattern-limited on-demand time, against the measured one."""
+    import ascetic_gb300 as A
+    A.lib()
+    ptr, col = A.rmat_csr(args.scale, args.edge_factor, args.seed)
+    srcs = pick_sources(ptr, 8, args.seed)
+    V = len(ptr) - 1
+    sizes = [16, 32, 48, 64, 96, 128, 192, 256, 512, 1024, 4096, 16384]
+    curve = {b: A.link_probe_runs(b) for b in sizes}
+    dma, smread = A.link_probe(1 << 30, 3)
+    xs = np.log(np.array(sizes, dtype=np.float64))
+    ys = np.array([curve[b] for b in sizes])
+
+    def rate(run_bytes):
+        return np.interp(np.log(np.clip(run_bytes, sizes[0], sizes[-1])), xs, ys)
+
+    deg = np.diff(ptr.astype(np.int64))
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=args.budget)) as g:
+        S = int(g.info.static_vertices)
+        eb = g.info.edge_bits / 8.0
+        nz = np.nonzero(deg > 0)[0]
+        nz = nz[nz >= S]
+        cs = np.concatenate([[0], np.cumsum(deg[nz])])
+        pred_s = meas_s = od_bytes = 0.0
+        runs_total = 0
+        for s in srcs:
+            lev, _ = g.run("bfs", s)
+            _, st = g.run("bfs", s, params=A.make_params(flags=A.RUN_NO_OUTPUT | A.RUN_PHASE_TIMING))
+            meas_s += st["ms_ondemand"] * 1e-3
+            lv = lev[nz]
+            for it in np.unique(lv):
+                if it >= V + 1:
+                    continue
+                act = (lv == it).astype(np.int8)
+                d = np.diff(np.concatenate([[0], act, [0]]))
+                starts, ends = np.nonzero(d == 1)[0], np.nonzero(d == -1)[0]
+                rb = (cs[ends] - cs[starts]) * eb
+                pred_s += float((rb / (rate(rb) * 1e9)).sum())
+                od_bytes += float(rb.sum())
+                runs_total += len(rb)
+    out = {"study": "host-link rate by run length; pattern-limited on-demand ceiling of the BFS",
+           "rmat_scale": args.scale, "budget_frac": args.budget, "edge_bits": int(eb * 8),
+           "sequential_peak_gbs": {"dma_h2d": round(dma, 1), "sm_reads": round(smread, 1)},
+           "runs_gbs_by_bytes": {str(b): round(curve[b], 1) for b in sizes},
+           "bfs_runs": len(srcs), "ondemand_bytes_per_bfs": int(od_bytes / len(srcs)),
+           "mean_run_bytes": round(od_bytes / max(runs_total, 1), 1),
+           "pattern_ceiling_gbs": round(od_bytes / pred_s / 1e9, 1) if pred_s else None,
+           "pattern_limited_ms_per_bfs": round(1e3 * pred_s / len(srcs), 3),
+           "measured_ondemand_ms_per_bfs": round(1e3 * meas_s / len(srcs), 3),
+           "measured_gbs": round(od_bytes / meas_s / 1e9, 1) if meas_s else None}
+    if pred_s and meas_s:
+        out["fraction_of_pattern_ceiling"] = round(pred_s / meas_s, 3)
+        out["fraction_of_sequential_peak"] = round(od_bytes / meas_s / 1e9 / dma, 3)
+    print(json.dumps(out), flush=True)
+
+
 def uvm_study(args):
     """The reference's UVM baseline (edges in managed memory, read-mostly, no
     static region) against the split engine at the same graph and sources:
@@ -382,6 +446,9 @@ def main():
         return
     if args.uvm_study:
         uvm_study(args)
+        return
+    if args.link_study:
+        link_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -314,6 +314,12 @@ asc_status asc_graph_rmat(uint32_t scale, uint32_t edge_factor, uint64_t seed, d
  * bandwidth of SM loads from mapped pinned host memory, in GB/s (1e9 B/s),
  * over a buffer of the given size (measurement helper, no reference counterpart). */
 asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double *sm_read_gbs);
+/* Host-link read rate (GB/s of requested bytes, best of iters) when every warp
+ * reads runs of run_bytes consecutive bytes at pseudo-random 4-byte-aligned
+ * offsets of a pinned, mapped buffer of `bytes`: the ceiling the on-demand
+ * expansion can reach for a given adjacency-list run length (short runs use
+ * 32-byte sectors and link requests partly). No reference counterpart. */
+asc_status asc_link_probe_runs(uint64_t bytes, uint32_t run_bytes, int iters, double *gbs);
 
 /* ---- allocation-free BFS ------------------------------------------------- */
 /* BFS over a CSR graph that the caller already holds in device memory, for

@@ -442,3 +442,12 @@ def test_bit_stream_widths(V):
                 assert np.array_equal(got, oracle.bfs(ptr, col, s)), (V, frac, s)
             got, _ = g.run("cc")
             assert np.array_equal(got, oracle.cc(ptr, col)), (V, frac)
+
+
+def test_link_probe_runs():
+    """The run-length link probe measures a positive rate and rejects bad sizes."""
+    assert A.link_probe_runs(64, nbytes=4 << 20, iters=1) > 0
+    assert A.link_probe_runs(4096, nbytes=4 << 20, iters=1) > 0
+    for bad in (2, 6, 1 << 20):
+        with pytest.raises(A.AscError):
+            A.link_probe_runs(bad, nbytes=4 << 20, iters=1)
