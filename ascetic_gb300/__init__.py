@@ -31,7 +31,7 @@ BFS, SSSP, CC, PR = range(4)
 BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES, BUDGET_MANAGED = range(6)
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
-RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP = 1, 2, 4, 8
+RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP, RUN_FRAGMENT_COUNTS = 1, 2, 4, 8, 16
 RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 
@@ -43,7 +43,7 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
             "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
             "asc_server_stats_get", "asc_server_destroy", "asc_graph_get_tuning", "asc_graph_set_tuning",
-            "asc_graph_tune", "asc_device_memory", "asc_link_probe_runs"]
+            "asc_graph_tune", "asc_device_memory", "asc_link_probe_runs", "asc_graph_fragment_counts"]
 TUNE_NO_CACHE = 1
 SERVE_BATCHED, SERVE_FIFO = 0, 1
 
@@ -164,6 +164,7 @@ def lib():
         "asc_write_graph": ([ctypes.c_char_p, ctypes.c_int, c_u64, c_u64, c_vp, c_vp, c_vp], ctypes.c_int),
         "asc_link_probe": ([c_u64, ctypes.c_int, P(c_dbl), P(c_dbl)], ctypes.c_int),
         "asc_link_probe_runs": ([c_u64, c_u32, ctypes.c_int, P(c_dbl)], ctypes.c_int),
+        "asc_graph_fragment_counts": ([c_vp, c_vp, c_u64, P(c_u64), ctypes.c_int], ctypes.c_int),
         "asc_bfs_device_noalloc": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, c_vp], ctypes.c_int),
         "asc_run_batch": ([c_vp, ctypes.c_int, c_vp, c_u32, P(Params), c_vp, P(Stats)], ctypes.c_int),
         "asc_server_config_default": ([P(ServerConfig)], None),
@@ -300,6 +301,15 @@ class Graph:
 
     def __exit__(self, *a):
         self.close()
+
+    def fragment_counts(self, reset=False):
+        """Edges read per 4096-edge fragment by the runs made with
+        RUN_FRAGMENT_COUNTS since the last reset (uint64 array)."""
+        n = ctypes.c_uint64(0)
+        _check(lib().asc_graph_fragment_counts(self._h, None, 0, ctypes.byref(n), 0))
+        out = np.zeros(max(n.value, 1), np.uint64)
+        _check(lib().asc_graph_fragment_counts(self._h, out.ctypes.data, n.value, None, 1 if reset else 0))
+        return out[:n.value]
 
     def refresh_info(self):
         _check(lib().asc_graph_info_get(self._h, ctypes.byref(self.info)))

@@ -71,6 +71,8 @@ struct Workspace {
     Tuning tune;
     int num_sms = 0;
     uint64_t device_bytes = 0;
+    unsigned long long *frag_counts = nullptr;  // per 4096-edge fragment, allocated on first use
+    unsigned long long *frag_active = nullptr;  // frag_counts during a counting run, else null
 };
 
 }  // namespace asc

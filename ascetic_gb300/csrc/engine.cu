@@ -95,7 +95,18 @@ struct RegionArgs {
     uint32_t dense_div;
     uint32_t wbits;               // > 0: u32 edges packed as (dst << wbits) | weight
     uint32_t ebits;               // bits per stored edge word: 32, or a bit stream of ebits per edge
+    unsigned long long *frag;     // non-null: add edges read per 4096-edge fragment
 };
+
+// Adds the n edges read from [b, b + n) to their 4096-edge fragments' counters.
+__device__ __forceinline__ void count_fragments(unsigned long long *frag, uint64_t b, uint32_t n) {
+    if (!n) return;
+    const uint64_t e = b + n;
+    for (uint64_t f = b >> 12; f <= (e - 1) >> 12; f++) {
+        const uint64_t lo = max(b, f << 12), hi = min(e, (f + 1) << 12);
+        atomicAdd(frag + f, (unsigned long long)(hi - lo));
+    }
+}
 
 // Edge layouts of the expansion kernels (their WORDS template argument):
 // 1 = one u32 per edge, 2 = {dst, weight} pairs, kBitsLayout = one word per
@@ -289,6 +300,7 @@ __device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem 
             act = false;
         }
         vu = a.val[u];
+        if (a.frag) count_fragments(a.frag, start, deg);
     }
     uint32_t total;
     uint32_t excl = block_excl_scan(deg, total, sm.warp);
@@ -389,6 +401,7 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
         if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+        if (a.frag) count_fragments(a.frag, b, n);
     }
 }
 
@@ -1094,6 +1107,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.dense_div = ws->tune.dense_div;
     a.wbits = g->wbits;
     a.ebits = g->edge_words == 1 ? g->ebits : 32;
+    a.frag = ws->frag_active;
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
     a.huge = ws->tune.huge_degree;
@@ -1311,6 +1325,7 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 
 void free_ws_buffers(Workspace *ws) {
     for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->far_bits,
+                    (void *)ws->frag_counts,
                     (void *)ws->bitmap[0],
                     (void *)ws->bitmap[1],
                     (void *)ws->queue[0],
@@ -1339,9 +1354,31 @@ void free_workspace(asc_graph *g) {
     g->ws = nullptr;
 }
 
+asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
+                              asc_stats *st);
+
+uint64_t fragment_count(const asc_graph *g) { return (g->E + 4095) / 4096; }
+
 asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
                          asc_stats *st) {
     ASC_TRY(ensure_workspace(g));
+    Workspace *ws = g->ws;
+    if (p.flags & ASC_RUN_FRAGMENT_COUNTS) {
+        if (!ws->frag_counts) {
+            const size_t bytes = 8 * std::max<uint64_t>(1, fragment_count(g));
+            ASC_CUDA(cudaMalloc(&ws->frag_counts, bytes));
+            ASC_CUDA(cudaMemsetAsync(ws->frag_counts, 0, bytes, g->stream));
+            ws->device_bytes += bytes;
+        }
+        ws->frag_active = ws->frag_counts;
+    }
+    const asc_status rc = run_traversal_impl(g, algo, source, p, out, st);
+    ws->frag_active = nullptr;
+    return rc;
+}
+
+asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
+                              asc_stats *st) {
     Workspace *ws = g->ws;
     const uint32_t V = (uint32_t)g->V;
     cudaStream_t s = g->stream;
@@ -1373,7 +1410,9 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
     launches += 3;
     ASC_CUDA(cudaGetLastError());
     const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
-    const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP));
+    // fragment counting runs the host-driven loop: the captured graph loop is
+    // built without counters
+    const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS));
     int iters = 0;
     double phase_ms[2] = {0, 0};
     if (use_graph) {
@@ -3189,3 +3228,22 @@ asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, 
 }
 
 }  // extern "C"
+
+extern "C" asc_status asc_graph_fragment_counts(asc_graph *g, uint64_t *out, uint64_t n, uint64_t *n_out, int reset) {
+    using namespace asc;
+    if (!g) return fail(ASC_ERR_INVALID, "asc_graph_fragment_counts: graph is NULL");
+    const uint64_t nf = fragment_count(g);
+    if (n_out) *n_out = nf;
+    Workspace *ws = g->ws;
+    const uint64_t k = std::min(n, nf);
+    if (!ws || !ws->frag_counts) {
+        if (out) memset(out, 0, 8 * k);
+        return ASC_OK;
+    }
+    if (out && k) {
+        ASC_CUDA(cudaMemcpyAsync(out, ws->frag_counts, 8 * k, cudaMemcpyDeviceToHost, g->stream));
+    }
+    if (reset) ASC_CUDA(cudaMemsetAsync(ws->frag_counts, 0, 8 * std::max<uint64_t>(1, nf), g->stream));
+    ASC_CUDA(cudaStreamSynchronize(g->stream));
+    return ASC_OK;
+}

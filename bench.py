@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
     ap.add_argument("--link-study", action="store_true",
                     help="host-link rate by run length and the BFS's pattern-limited on-demand ceiling")
+    ap.add_argument("--fragment-study", action="store_true",
+                    help="edge reads per 4096-edge fragment: what a fragment cache could move off the link")
     ap.add_argument("--uvm-study", action="store_true",
                     help="compare BFS on the managed-memory (UVM) engine with the split engine")
     return ap.parse_args()
@@ -368,6 +370,47 @@ def link_study(args):
     print(json.dumps(out), flush=True)
 
 
+def fragment_study(args):
+    """Would a cache of hot edge fragments (the reference's fragment swap) cut
+    link bytes? Counts the edges every run reads per 4096-edge fragment
+    (RUN_FRAGMENT_COUNTS) for BFS and SSSP from 4 sources each and one CC run on
+    the symmetrised graph, then compares the share of reads the static prefix
+    serves with the share the best possible set of the same number of fragments,
+    chosen with hindsight, would serve."""
+    import ascetic_gb300 as A
+    A.lib()
+    prm = A.make_params(flags=A.RUN_NO_OUTPUT | A.RUN_FRAGMENT_COUNTS)
+    out = {"study": "edge reads per 4096-edge fragment; static prefix vs best resident set",
+           "rmat_scale": args.scale, "budget_frac": args.budget}
+    ptr, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
+    srcs = pick_sources(ptr, 4, args.seed)
+    legs = [("bfs", ptr, adj[:, 0].copy(), srcs), ("sssp", ptr, adj, srcs)]
+    del adj
+    for algo, p_, e_, ss in legs:
+        with A.Graph.from_csr(p_, e_, budget=A.make_budget(frac=args.budget)) as g:
+            for s_ in ss:
+                g.run(algo, s_, params=prm)
+            out[algo] = _fragment_shares(g)
+    del legs
+    sptr, scol = A.rmat_csr(args.scale, args.edge_factor, args.seed, symmetric=True)
+    with A.Graph.from_csr(sptr, scol, budget=A.make_budget(frac=args.budget)) as g:
+        g.run("cc", params=prm)
+        out["cc"] = _fragment_shares(g)
+    print(json.dumps(out), flush=True)
+
+
+def _fragment_shares(g):
+    c = g.fragment_counts(reset=True).astype(np.float64)
+    k = int(g.info.static_edges) // 4096
+    tot = c.sum()
+    prefix = c[:k].sum() / tot if tot else 0.0
+    best = np.sort(c)[::-1][:k].sum() / tot if tot else 0.0
+    return {"edges_read": int(tot), "fragments": len(c), "resident_fragments": k,
+            "edge_bits": int(g.info.edge_bits), "static_prefix_share": round(prefix, 4),
+            "best_resident_share": round(best, 4),
+            "link_bytes_saved_at_best": round((best - prefix) / (1 - prefix), 4) if prefix < 1 else 0.0}
+
+
 def uvm_study(args):
     """The reference's UVM baseline (edges in managed memory, read-mostly, no
     static region) against the split engine at the same graph and sources:
@@ -449,6 +492,9 @@ def main():
         return
     if args.link_study:
         link_study(args)
+        return
+    if args.fragment_study:
+        fragment_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -123,8 +123,11 @@ enum {
     ASC_RUN_DEVICE_OUT = 1u << 1,  /* out is a device pointer */
     ASC_RUN_PHASE_TIMING = 1u << 2, /* time static and on-demand kernels separately (CUDA events);
                                        implies a host-driven iteration loop */
-    ASC_RUN_HOST_LOOP = 1u << 3     /* drive iterations from the host (one readback per iteration)
+    ASC_RUN_HOST_LOOP = 1u << 3,    /* drive iterations from the host (one readback per iteration)
                                        instead of the CUDA-graph loop */
+    ASC_RUN_FRAGMENT_COUNTS = 1u << 4 /* BFS/SSSP/CC: add the edges this run reads to per-fragment
+                                         counters (4096 edges a fragment; read them with
+                                         asc_graph_fragment_counts); implies ASC_RUN_HOST_LOOP */
 };
 
 typedef struct asc_params {
@@ -314,6 +317,14 @@ asc_status asc_graph_rmat(uint32_t scale, uint32_t edge_factor, uint64_t seed, d
  * bandwidth of SM loads from mapped pinned host memory, in GB/s (1e9 B/s),
  * over a buffer of the given size (measurement helper, no reference counterpart). */
 asc_status asc_link_probe(uint64_t bytes, int iters, double *dma_h2d_gbs, double *sm_read_gbs);
+/* Edges read per fragment of the edge array (fragment f holds edges
+ * [4096 f, 4096 f + 4096)), summed over the runs made with
+ * ASC_RUN_FRAGMENT_COUNTS since the last reset: the visit counters of the
+ * reference's fragment swap (gpu_kernels.cu:666-739), kept as a measurement of
+ * where reads fall. out receives min(n, ceil(E / 4096)) entries; *n_out (if not
+ * NULL) the number of fragments. reset != 0 clears the counters afterwards. */
+asc_status asc_graph_fragment_counts(asc_graph *g, uint64_t *out, uint64_t n, uint64_t *n_out, int reset);
+
 /* Host-link read rate (GB/s of requested bytes, best of iters) when every warp
  * reads runs of run_bytes consecutive bytes at pseudo-random 4-byte-aligned
  * offsets of a pinned, mapped buffer of `bytes`: the ceiling the on-demand

@@ -451,3 +451,23 @@ def test_link_probe_runs():
     for bad in (2, 6, 1 << 20):
         with pytest.raises(A.AscError):
             A.link_probe_runs(bad, nbytes=4 << 20, iters=1)
+
+
+def test_fragment_counts_add_up():
+    """Per-fragment read counters sum to the edges the runs processed, and
+    counting leaves the values unchanged."""
+    ptr, col = A.rmat_csr(13, 16, 71)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.3)) as g:
+        prm = A.make_params(flags=A.RUN_FRAGMENT_COUNTS)
+        total = 0
+        for s in (0, 5):
+            got, st = g.run("bfs", s, params=prm)
+            assert np.array_equal(got, oracle.bfs(ptr, col, s))
+            total += st["edges_processed"]
+        got, st = g.run("cc", params=prm)
+        total += st["edges_processed"]
+        c = g.fragment_counts(reset=True)
+        assert len(c) == (g.E + 4095) // 4096 and int(c.sum()) == total
+        assert g.fragment_counts().sum() == 0  # the reset cleared them
+        g.run("bfs", 0)  # without the flag nothing is counted
+        assert g.fragment_counts().sum() == 0
