@@ -36,7 +36,7 @@ constexpr int kBlock = 256;
 struct Tuning {
     uint32_t huge_degree = 512;   // lists longer than this are cut into segments
     uint32_t segment_edges = 2048;  // edges per segment work item
-    uint32_t ctas_per_sm = 4;     // persistent expansion grid = SMs x this
+    uint32_t ctas_per_sm = 0;     // persistent expansion grid = SMs x this (0: as many as stay resident)
     uint32_t dense_div = 64;      // walk a region in id order (frontier bitmap) when its list
                                   // holds more than 1/dense_div of the region's vertices; 0 = never
     uint32_t delta = 0;           // SSSP near-far step: distances >= threshold wait in the far set,

@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--quick", action="store_true", help="BFS only (skip SSSP/CC legs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default thresholds instead of autotuning each graph before its timed runs")
     ap.add_argument("--split", action="store_true",
                     help="profiling aid: time the steps with one launch per region (phase timing)")
     ap.add_argument("--batch", type=int, default=64,
@@ -305,7 +307,8 @@ def workload_config(args):
                         "capped at %d%% of edge bytes, rest read on demand from pinned host memory"
                         % (args.scale, args.edge_factor, args.seed, round(100 * args.budget)),
             "scale": args.scale, "edge_factor": args.edge_factor, "seed": args.seed, "budget_frac": args.budget,
-            "l2": "inputs larger than L2 (edge array %.2f GB)" % (4.0 * (1 << args.scale) * args.edge_factor / 1e9)}
+            "l2": "inputs larger than L2 (edge array %.2f GB as 32-bit words)"
+                  % (4.0 * (1 << args.scale) * args.edge_factor / 1e9)}
 
 
 def link_study(args):
@@ -515,6 +518,11 @@ def main():
     budget = A.make_budget(frac=args.budget)
     g = A.Graph.from_csr(ptr, col, budget=budget)
     info = g.info
+    # the autotuner picks the thresholds on sources other than the timed ones
+    tune_srcs = pick_sources(ptr, 4, args.seed + 1000)
+    t_tune = time.time()
+    tuning = None if args.no_tune else g.tune("bfs", tune_srcs, cache=False)
+    t_tune = time.time() - t_tune
     nores = A.make_params(flags=A.RUN_NO_OUTPUT)
     for i in range(args.warmup):
         g.run("bfs", srcs[i % 8], params=A.make_params(flags=A.RUN_NO_OUTPUT))
@@ -604,7 +612,9 @@ def main():
     line = {"metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(tot_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic RMAT (seeded)",
-            "config": workload_config(args), "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "config": dict(workload_config(args), tuning=tuning and {k: tuning[k] for k in (
+                "huge_degree", "segment_edges", "dense_div", "ctas_per_sm")}, tuning_s=round(t_tune, 2)),
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "roofline": roofline, "roofline_static_hbm": roof_static, "roofline_ondemand_link": roof_link,
             "graph": {"V": V, "E": int(g.E), "edge_bits": int(info.edge_bits), "static_edges": int(info.static_edges),
                       "static_vertices": int(info.static_vertices), "device_edge_bytes": int(info.device_edge_bytes),
@@ -653,6 +663,8 @@ def main():
         extra = {}
         _, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
         with A.Graph.from_csr(ptr, adj, budget=budget) as gw:
+            if not args.no_tune:
+                gw.tune("sssp", tune_srcs[:2], cache=False)
             gw.run("sssp", srcs[0], params=A.make_params(flags=A.RUN_NO_OUTPUT))
             e, ms, proc, its = 0, 0.0, 0, 0
             for s in srcs[:4]:
@@ -669,6 +681,9 @@ def main():
         del adj
         sp, sc = A.rmat_csr(args.scale, args.edge_factor, args.seed, symmetric=True)
         with A.Graph.from_csr(sp, sc, budget=budget) as gs:
+            if not args.no_tune:
+                gs.tune("cc", cache=False)
+            extra["cc_tuning"] = None if args.no_tune else gs.get_tuning()
             _, st = gs.run("cc", params=A.make_params(flags=A.RUN_NO_OUTPUT))
             _, st = gs.run("cc", params=A.make_params(flags=A.RUN_NO_OUTPUT))
             extra["cc_ms"] = round(st["ms_total"], 3)
