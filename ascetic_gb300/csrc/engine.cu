@@ -1878,10 +1878,50 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 // segment of a long list); lanes are sources (two 32-source halves). Edges are
 // loaded 32 at a time, coalesced, and broadcast with shuffles; the 64
 // distances of a destination are one 256-byte row.
+#ifndef ASC_MS_SSSP_SPARSE
+#define ASC_MS_SSSP_SPARSE 8
+#endif
+// A frontier vertex active for at most this many sources relaxes its edges
+// lanes-per-edge (one pass per active source) instead of lanes-per-source
+// (64-source batch on RMAT scale 24: 160 ms never, 142 ms at <= 8, 143 at
+// <= 16, 156 at <= 32, 292 always).
+constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
+
 __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs &a, uint32_t u, uint64_t b,
                                               uint32_t n) {
     const int lane = threadIdx.x & 31;
     const unsigned long long f = m.front[u];
+    if (__popcll(f) <= kMsSparseSources) {
+        // few sources: each lane takes one edge and relaxes it for every active
+        // source, so a warp instruction covers 32 edges instead of one
+        for (uint32_t c = 0; c < n; c += 32) {
+            const bool ok = c + lane < n;
+            uint32_t v = 0, w = 0;
+            if (ok) {
+                if (a.wbits) {
+                    const uint32_t e = edge_word(a.edges, b + c + lane, a.ebits);
+                    v = e >> a.wbits;
+                    w = e & ((1u << a.wbits) - 1u);
+                } else {
+                    const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
+                    v = e.x;
+                    w = e.y;
+                }
+            }
+            uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+            unsigned long long imp = 0;
+            for (unsigned long long fm = f; fm; fm &= fm - 1) {
+                const int s = __ffsll((long long)fm) - 1;
+                const uint32_t ds = m.dist[(uint64_t)u * kMaxBatch + s];
+                if (ok) {
+                    const uint32_t nd = ds + w;
+                    if (nd < row[s] && nd < atomicMin(&row[s], nd)) imp |= 1ull << s;
+                }
+            }
+            if (imp) mark_touched(m, atomicOr(&m.next[v], imp) == 0ull, v);
+        }
+        return;
+    }
     const bool lo_on = (f >> lane) & 1ull, hi_on = (f >> (lane + 32)) & 1ull;
     const uint32_t d_lo = lo_on ? m.dist[(uint64_t)u * kMaxBatch + lane] : 0;
     const uint32_t d_hi = hi_on ? m.dist[(uint64_t)u * kMaxBatch + lane + 32] : 0;
