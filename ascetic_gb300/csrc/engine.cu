@@ -47,6 +47,16 @@ constexpr unsigned kFull = 0xffffffffu;
 // 8 x 256 threads fill an SM, 32 registers each. Measured on RMAT scale 24 with
 // bit-packed edges: 65.6 GTEPS at 8, 64.5 at 6, 57.3 at 4 (64 registers, half
 // the warps: the loads over the host link want every warp the SM can hold).
+// The same for the PageRank pull/scatter kernels (8: FP32 standard PageRank on
+// RMAT scale 23 in 181 ms against 195 at the compiler's choice of 40 registers)
+// and the 64-source batch kernels (left to the compiler: at 6 or 8 the batched
+// SSSP kernel spills).
+#ifndef ASC_PR_MIN_BLOCKS
+#define ASC_PR_MIN_BLOCKS 8
+#endif
+#ifndef ASC_MS_MIN_BLOCKS
+#define ASC_MS_MIN_BLOCKS 1
+#endif
 #ifndef ASC_EXPAND_MIN_BLOCKS
 #define ASC_EXPAND_MIN_BLOCKS 8
 #endif
@@ -903,7 +913,7 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
 }
 
 template <typename T, bool REF>
-__global__ void __launch_bounds__(kBlock) pr_pull_kernel(PrArgs<T> p) {
+__global__ void __launch_bounds__(kBlock, ASC_PR_MIN_BLOCKS) pr_pull_kernel(PrArgs<T> p) {
     __shared__ PrSmem<T> sm;
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
@@ -1847,7 +1857,7 @@ __device__ __forceinline__ void ms_item(const MsArgs &m, const RegionArgs &a, ui
 }
 
 template <int WORDS>
-__global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
+__global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_bfs_expand_kernel(MsArgs m) {
     __shared__ MsSmem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
     bool m0, m1;
@@ -2001,7 +2011,7 @@ __device__ __forceinline__ void ms_sssp_item(const MsArgs &m, const RegionArgs &
 // Work items are per warp and handed out 8 at a time: [static segments and
 // list vertices][on-demand segments and list vertices]. The SSSP batch always
 // builds lists (its RegionArgs carry dense_div = 0).
-__global__ void __launch_bounds__(kBlock) ms_sssp_expand_kernel(MsArgs m) {
+__global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_sssp_expand_kernel(MsArgs m) {
     const uint32_t n0 = m.r0.cnt_in[0], s0 = m.r0.cnt_in[2];
     const uint32_t n1 = m.r1.cnt_in[1], s1 = m.r1.cnt_in[3];
     const uint32_t t0 = s0 + n0, total = t0 + s1 + n1;
@@ -2512,7 +2522,7 @@ __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t
 }
 
 template <typename T, int WORDS>
-__global__ void __launch_bounds__(kBlock) pr_scatter_kernel(PushArgs<T> p) {
+__global__ void __launch_bounds__(kBlock, ASC_PR_MIN_BLOCKS) pr_scatter_kernel(PushArgs<T> p) {
     __shared__ PushSmem<T> sm;
     const uint32_t s0 = p.r0.cnt_in[2], s1 = p.r1.cnt_in[3];
     const uint32_t t0 = s0 + (p.r0.dense_end - p.r0.dense_begin + kBlock - 1) / kBlock;
