@@ -43,7 +43,8 @@ EXPORTED = ["asc_status_string", "asc_last_error", "asc_version", "asc_device_co
             "asc_bfs_device_noalloc", "asc_run_batch", "asc_server_config_default", "asc_server_create",
             "asc_server_add_graph", "asc_server_submit", "asc_server_wait", "asc_server_cancel",
             "asc_server_stats_get", "asc_server_destroy", "asc_graph_get_tuning", "asc_graph_set_tuning",
-            "asc_graph_tune", "asc_device_memory", "asc_link_probe_runs", "asc_graph_fragment_counts"]
+            "asc_graph_tune", "asc_device_memory", "asc_link_probe_runs", "asc_graph_fragment_counts",
+            "asc_host_alloc", "asc_host_free"]
 TUNE_NO_CACHE = 1
 SERVE_BATCHED, SERVE_FIFO = 0, 1
 
@@ -146,6 +147,8 @@ def lib():
         "asc_version": ([], ctypes.c_char_p),
         "asc_device_count": ([], ctypes.c_int),
         "asc_device_memory": ([P(c_u64), P(c_u64)], ctypes.c_int),
+        "asc_host_alloc": ([c_u64, P(c_vp)], ctypes.c_int),
+        "asc_host_free": ([c_vp], ctypes.c_int),
         "asc_budget_default": ([P(Budget)], None),
         "asc_graph_open": ([ctypes.c_char_p, ctypes.c_int, P(Budget), gpp], ctypes.c_int),
         "asc_graph_from_csr": ([c_u64, c_u64, c_vp, c_vp, c_u32, c_vp, P(Budget), gpp], ctypes.c_int),
@@ -200,6 +203,31 @@ def _check(status):
 
 def device_count():
     return lib().asc_device_count()
+
+
+class PinnedArray:
+    """A numpy array over page-locked host memory (asc_host_alloc), for result
+    buffers that asc_run fills at the copy engine's full rate. Keep the object
+    alive while the array is in use; close() frees the memory."""
+
+    def __init__(self, n, dtype=np.uint32):
+        dtype = np.dtype(dtype)
+        self._p = ctypes.c_void_p()
+        _check(lib().asc_host_alloc(max(1, n * dtype.itemsize), ctypes.byref(self._p)))
+        buf = (ctypes.c_char * max(1, n * dtype.itemsize)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=n)
+
+    def close(self):
+        if self._p and self._p.value:
+            self.array = None
+            lib().asc_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def device_free_bytes():

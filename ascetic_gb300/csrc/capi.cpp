@@ -100,6 +100,24 @@ int asc_device_count(void) {
     return n;
 }
 
+asc_status asc_host_alloc(uint64_t bytes, void **ptr) {
+    if (!ptr) return fail(ASC_ERR_INVALID, "asc_host_alloc: ptr is NULL");
+    *ptr = nullptr;
+    const cudaError_t e = cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        cudaGetLastError();
+        return fail(ASC_ERR_NOMEM, "cudaHostAlloc of %llu bytes failed: %s", (unsigned long long)bytes,
+                    cudaGetErrorString(e));
+    }
+    return ASC_OK;
+}
+
+asc_status asc_host_free(void *ptr) {
+    if (ptr) ASC_CUDA(cudaFreeHost(ptr));
+    return ASC_OK;
+}
+
 asc_status asc_device_memory(uint64_t *free_bytes, uint64_t *total_bytes) {
     size_t f = 0, t = 0;
     ASC_CUDA(cudaMemGetInfo(&f, &t));

@@ -168,6 +168,11 @@ const char *asc_version(void);
 int asc_device_count(void);
 /* Free and total bytes of the current CUDA device (cudaMemGetInfo). */
 asc_status asc_device_memory(uint64_t *free_bytes, uint64_t *total_bytes);
+/* Page-locked host memory for result buffers: asc_run copies values into it at
+ * the copy engine's full rate instead of through a pageable staging path.
+ * Free it with asc_host_free. */
+asc_status asc_host_alloc(uint64_t bytes, void **ptr);
+asc_status asc_host_free(void *ptr);
 
 /* ---- graphs -------------------------------------------------------------- */
 void asc_budget_default(asc_budget *b);

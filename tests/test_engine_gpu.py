@@ -471,3 +471,14 @@ def test_fragment_counts_add_up():
         assert g.fragment_counts().sum() == 0  # the reset cleared them
         g.run("bfs", 0)  # without the flag nothing is counted
         assert g.fragment_counts().sum() == 0
+
+
+def test_pinned_result_buffer():
+    """asc_run fills a page-locked buffer from asc_host_alloc like any other."""
+    ptr, col = A.rmat_csr(12, 16, 81)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=0.3)) as g:
+        buf = A.PinnedArray(g.V, np.uint32)
+        for s in (0, 9):
+            g.run("bfs", s, out=buf.array)
+            assert np.array_equal(buf.array, oracle.bfs(ptr, col, s))
+        buf.close()
