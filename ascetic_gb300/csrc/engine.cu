@@ -2030,57 +2030,69 @@ __global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_sssp_expand_kern
     }
 }
 
-// Apply pass (one thread per word of the touched bitmap): the new sources of a
-// touched vertex become its frontier mask, BFS levels are written into the
+// Apply pass over the touched bitmap: the new sources of a touched vertex
+// become its frontier mask, BFS levels are written into the
 // sources' planes, and the vertex's bit goes into the next frontier bitmap
 // (with per-region counts for the compaction kernel). ORs every new mask into
 // *alive so finished sources can be told apart.
 template <bool BFS>
 __global__ void ms_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_off, uint32_t it,
                                 unsigned long long *alive, uint32_t nwords) {
+    // a warp takes 32 touched-bitmap words at a time and walks the non-empty
+    // ones, lane = vertex: the level stores of one source go to 32 consecutive
+    // entries of its plane (one coalesced store per source present in the word)
     const RegionArgs &a = m.r0;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long any = 0;
     uint32_t n0 = 0, n1 = 0;
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
-        uint32_t word = m.touched[w];
-        if (!word) continue;
-        m.touched[w] = 0;
-        uint32_t nbits = 0;
-        while (word) {
-            const int b = __ffs(word) - 1;
-            word &= word - 1;
-            const uint32_t v = 32 * w + b;
-            unsigned long long nb = m.next[v];
-            m.next[v] = 0;
+    for (uint64_t g0 = (uint64_t)warp * 32; g0 < nwords; g0 += (uint64_t)nwarps * 32) {
+        const uint64_t gw = g0 + lane;
+        const uint32_t tw = gw < nwords ? m.touched[gw] : 0u;
+        unsigned nz = __ballot_sync(kFull, tw != 0);
+        while (nz) {
+            const int j = __ffs(nz) - 1;
+            nz &= nz - 1;
+            const uint32_t w = (uint32_t)g0 + (uint32_t)j;
+            const uint32_t word = __shfl_sync(kFull, tw, j);
+            const uint32_t v = 32 * w + lane;
+            unsigned long long nb = 0;
+            if ((word >> lane) & 1u) {
+                nb = m.next[v];
+                m.next[v] = 0;
+                if (BFS) {
+                    nb &= ~m.visit[v];
+                    m.visit[v] |= nb;
+                }
+                m.front[v] = nb;
+                any |= nb;
+            }
             if (BFS) {
-                nb &= ~m.visit[v];
-                m.visit[v] |= nb;
-                unsigned long long t = nb;
-                while (t) {
-                    const int s = __ffsll((long long)t) - 1;
-                    t &= t - 1;
-                    planes[s][v] = (uint32_t)((int32_t)it + lvl_off[s]);
+                unsigned long long un = ((unsigned long long)__reduce_or_sync(kFull, (uint32_t)(nb >> 32)) << 32) |
+                                        __reduce_or_sync(kFull, (uint32_t)nb);
+                while (un) {
+                    const int src = __ffsll((long long)un) - 1;
+                    un &= un - 1;
+                    if ((nb >> src) & 1ull) planes[src][v] = (uint32_t)((int32_t)it + lvl_off[src]);
                 }
             }
-            m.front[v] = nb;
-            any |= nb;
-            if (nb) nbits |= 1u << b;
-        }
-        if (nbits) {
-            a.bitmap[w] = nbits;
-            const uint32_t v0 = 32 * w;
-            const uint32_t smask = v0 + 32 <= a.S ? 0xffffffffu : (v0 >= a.S ? 0 : (1u << (a.S - v0)) - 1u);
-            n0 += __popc(nbits & smask);
-            n1 += __popc(nbits & ~smask);
+            const unsigned nbits = __ballot_sync(kFull, nb != 0ull);
+            if (lane == 0) {
+                m.touched[w] = 0;
+                if (nbits) {
+                    a.bitmap[w] = nbits;
+                    const uint32_t v0 = 32 * w;
+                    const uint32_t smask =
+                        v0 + 32 <= a.S ? 0xffffffffu : (v0 >= a.S ? 0 : (1u << (a.S - v0)) - 1u);
+                    n0 += __popc(nbits & smask);
+                    n1 += __popc(nbits & ~smask);
+                }
+            }
         }
     }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        any |= __shfl_down_sync(kFull, any, d);
-        n0 += __shfl_down_sync(kFull, n0, d);
-        n1 += __shfl_down_sync(kFull, n1, d);
-    }
-    if ((threadIdx.x & 31) == 0) {
+    for (int d = 16; d > 0; d >>= 1) any |= __shfl_down_sync(kFull, any, d);
+    if (lane == 0) {
         if (any) atomicOr(alive, any);
         if (n0) atomicAdd(&a.cnt_out[6], n0);
         if (n1) atomicAdd(&a.cnt_out[7], n1);
