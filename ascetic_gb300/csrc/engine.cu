@@ -1857,7 +1857,7 @@ __device__ __forceinline__ void ms_item(const MsArgs &m, const RegionArgs &a, ui
 }
 
 template <int WORDS>
-__global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_bfs_expand_kernel(MsArgs m) {
+__global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
     __shared__ MsSmem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
     bool m0, m1;
@@ -1925,17 +1925,25 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
                 const uint32_t ds = m.dist[(uint64_t)u * kMaxBatch + s];
                 if (ok) {
                     const uint32_t nd = ds + w;
-                    if (nd < row[s] && nd < atomicMin(&row[s], nd)) imp |= 1ull << s;
+                    if (nd < row[s]) {
+                        atomicMin(&row[s], nd);  // fire-and-forget, as in the dense path below
+                        imp |= 1ull << s;
+                    }
                 }
             }
-            if (imp) mark_touched(m, atomicOr(&m.next[v], imp) == 0ull, v);
+            if (imp) {
+                atomicOr(&m.next[v], imp);
+                atomicOr(&m.touched[v >> 5], 1u << (v & 31));
+            }
         }
         return;
     }
-    const bool lo_on = (f >> lane) & 1ull, hi_on = (f >> (lane + 32)) & 1ull;
-    const uint32_t d_lo = lo_on ? m.dist[(uint64_t)u * kMaxBatch + lane] : 0;
-    const uint32_t d_hi = hi_on ? m.dist[(uint64_t)u * kMaxBatch + lane + 32] : 0;
-    const bool any_hi = (f >> 32) != 0;
+    // many sources: each half-warp takes one edge, each of its 16 lanes four
+    // sources (one 16-byte load of the destination's distance row per lane),
+    // so a warp relaxes two edges per pass
+    const uint32_t half = (uint32_t)lane >> 4, l = (uint32_t)lane & 15u;
+    const uint4 du = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * kMaxBatch)[l];
+    const uint32_t act4 = (uint32_t)(f >> (4 * l)) & 0xfu;
     for (uint32_t c = 0; c < n; c += 32) {
         uint32_t ev = 0, ew = 0;
         if (c + lane < n) {
@@ -1950,36 +1958,31 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
             }
         }
         const uint32_t cn = min(32u, n - c);
-        // four edges at a time: their distance-row reads are in flight together
-        for (uint32_t j0 = 0; j0 < cn; j0 += 4) {
-            uint32_t vv[4], ww[4], clo[4], chi[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const uint32_t j = j0 + k;
-                vv[k] = __shfl_sync(kFull, ev, j & 31);
-                ww[k] = __shfl_sync(kFull, ew, j & 31);
-                const bool ok = j < cn;
-                const uint32_t *row = m.dist + (uint64_t)vv[k] * kMaxBatch;
-                clo[k] = (ok && lo_on) ? row[lane] : 0;
-                chi[k] = (ok && any_hi && hi_on) ? row[lane + 32] : 0;
+        for (uint32_t j0 = 0; j0 < cn; j0 += 2) {
+            const uint32_t j = j0 + half;
+            const uint32_t v = __shfl_sync(kFull, ev, j & 31), w = __shfl_sync(kFull, ew, j & 31);
+            const bool ok = j < cn;
+            uint32_t imp = 0;
+            if (ok && act4) {
+                uint32_t *row = m.dist + (uint64_t)v * kMaxBatch + 4 * l;
+                const uint4 cur = *reinterpret_cast<const uint4 *>(row);
+                const uint32_t nd0 = du.x + w, nd1 = du.y + w, nd2 = du.z + w, nd3 = du.w + w;
+                // the lowering is fire-and-forget: a source whose value another
+                // thread lowered further in the meantime is marked active for v
+                // all the same, which costs at most a relaxation of v with its
+                // current distance and never changes the fixpoint
+                if ((act4 & 1u) && nd0 < cur.x) { atomicMin(row + 0, nd0); imp |= 1u; }
+                if ((act4 & 2u) && nd1 < cur.y) { atomicMin(row + 1, nd1); imp |= 2u; }
+                if ((act4 & 4u) && nd2 < cur.z) { atomicMin(row + 2, nd2); imp |= 4u; }
+                if ((act4 & 8u) && nd3 < cur.w) { atomicMin(row + 3, nd3); imp |= 8u; }
             }
+            // the half-warp's improved sources as one 64-bit mask
+            unsigned long long im = (unsigned long long)imp << (4 * l);
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (j0 + k >= cn) break;
-                const uint32_t v = vv[k], w = ww[k];
-                uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
-                bool imp_lo = false, imp_hi = false;
-                if (lo_on) {
-                    const uint32_t nd = d_lo + w;
-                    if (nd < clo[k]) imp_lo = nd < atomicMin(&row[lane], nd);
-                }
-                if (any_hi && hi_on) {
-                    const uint32_t nd = d_hi + w;
-                    if (nd < chi[k]) imp_hi = nd < atomicMin(&row[lane + 32], nd);
-                }
-                const unsigned blo = __ballot_sync(kFull, imp_lo), bhi = __ballot_sync(kFull, imp_hi);
-                if ((blo | bhi) && lane == 0)
-                    mark_touched(m, atomicOr(&m.next[v], ((unsigned long long)bhi << 32) | blo) == 0ull, v);
+            for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
+            if (l == 0 && ok && im) {
+                atomicOr(&m.next[v], im);
+                atomicOr(&m.touched[v >> 5], 1u << (v & 31));
             }
         }
     }
