@@ -277,11 +277,17 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
         return true;
     }
     if (nv >= cur) return false;
-    uint32_t old = atomicMin(&a.val[v], nv);
-    if (nv >= old) return false;
-    if (ALG == kSSSP && a.far_bits && nv >= *a.thresh) {
-        atomicOr(&a.far_bits[v >> 5], bit);  // waits until the threshold reaches it
-        return false;
+    if (ALG == kSSSP && a.far_bits) {
+        uint32_t old = atomicMin(&a.val[v], nv);
+        if (nv >= old) return false;
+        if (nv >= *a.thresh) {
+            atomicOr(&a.far_bits[v >> 5], bit);  // waits until the threshold reaches it
+            return false;
+        }
+    } else {
+        // fire-and-forget: if another thread lowered v further since the probe,
+        // it set v's bit too, so the next frontier is the same either way
+        atomicMin(&a.val[v], nv);
     }
     return (atomicOr(&a.bitmap[v >> 5], bit) & bit) == 0;
 }
