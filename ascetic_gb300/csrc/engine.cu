@@ -1031,10 +1031,11 @@ __global__ void seed_huge_segments_kernel(RegionArgs a, const uint32_t *huge_lis
 
 // --------------------------------------------------------------- host -------
 
-// Sizes and allocates the frontier machinery of one run for graph g.
-asc_status alloc_workspace(asc_graph *g, Workspace *ws) {
+// Sizes and allocates the frontier machinery of one run for graph g, with
+// the graph's tuning or (graph_tuning false) the default thresholds.
+asc_status alloc_workspace(asc_graph *g, Workspace *ws, bool graph_tuning = true) {
     ws->V = g->V;
-    if (g->has_tuning) ws->tune = g->tuning;
+    if (g->has_tuning && graph_tuning) ws->tune = g->tuning;
     ASC_CUDA(cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, g->device));
     {
         // persistent grids fill the GPU: as many CTAs per SM as stay resident
@@ -2217,7 +2218,9 @@ asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **
     b->sssp = sssp;
     b->stride = stride;
     asc_status st = stride == 64 ? ASC_OK : fail(ASC_ERR_UNSUPPORTED, "batch rows of %u sources", stride);
-    if (st == ASC_OK) st = alloc_workspace(g, &b->ws);
+    // 64-source batches keep the default thresholds: a graph's tuning is chosen on
+    // single-source runs, and the batch kernels measured faster with the defaults
+    if (st == ASC_OK) st = alloc_workspace(g, &b->ws, false);
     if (sssp) b->ws.tune.dense_div = 0;  // the SSSP batch walks lists only
     const uint64_t V = g->V;
     auto al = [&](void **p, size_t n) {

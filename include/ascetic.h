@@ -222,7 +222,8 @@ asc_status asc_pr_opt(const char *path, double advise_rate, double *out, asc_sta
  * than 1/dense_div of its vertices is walked in id order through the frontier
  * bitmap (0: never); ctas_per_sm sizes the persistent grids (0: as many as stay
  * resident); delta is the SSSP near-far step. ms is the measured time per run of the chosen setting (-1 when
- * it came from the cache). No reference counterpart (its launch shape is fixed
+ * it came from the cache). They apply to single-source runs; 64-source batches
+ * keep the defaults. No reference counterpart (its launch shape is fixed
  * at 56 x 1024, GraphMeta.cuh:55-56). */
 typedef struct asc_tuning {
     uint32_t huge_degree, segment_edges, dense_div, ctas_per_sm;
