@@ -191,46 +191,6 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t &total,
     return s_warp[w] + incl - x;
 }
 
-// Appends the vertices whose bit this warp won to the next frontier. Every lane
-// of the warp calls it (won = false where there is nothing to add).
-__device__ __forceinline__ void push_warp(const RegionArgs &a, bool won, uint32_t v) {
-    if (!__any_sync(kFull, won)) return;
-    uint32_t deg = 0;
-    bool od = false, huge = false;
-    if (won) {
-        uint32_t b = a.ptr[v];
-        deg = a.ptr[v + 1] - b;
-        od = v >= a.S;
-        huge = deg > a.huge;
-    }
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const unsigned ms = __ballot_sync(kFull, won && !huge && !od);
-    const unsigned mo = __ballot_sync(kFull, won && !huge && od);
-    uint32_t bs = 0, bo = 0;
-    if (ms) {
-        int l = __ffs(ms) - 1;
-        if (lane == l) bs = atomicAdd(&a.cnt_out[0], (uint32_t)__popc(ms));
-        bs = __shfl_sync(kFull, bs, l);
-    }
-    if (mo) {
-        int l = __ffs(mo) - 1;
-        if (lane == l) bo = atomicAdd(&a.cnt_out[1], (uint32_t)__popc(mo));
-        bo = __shfl_sync(kFull, bo, l);
-    }
-    if (won) {
-        if (!huge) {
-            if (!od) a.q_out[bs + __popc(ms & lt)] = v;
-            else a.q_out[a.S + bo + __popc(mo & lt)] = v;
-        } else {
-            uint32_t nseg = (deg + a.seg_len - 1) / a.seg_len;
-            uint32_t base = atomicAdd(&a.cnt_out[2 + od], nseg);
-            uint64_t *dst = a.seg_out + (od ? a.segcap_static : 0) + base;
-            for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
-        }
-    }
-}
-
 template <int ALG, int WORDS>
 __device__ __forceinline__ void load_edge(const RegionArgs &a, uint32_t vu, uint64_t idx, uint32_t &v, uint32_t &nv) {
     if (WORDS == 2) {
@@ -691,22 +651,6 @@ template <int ALG>
 __global__ void init_values_kernel(uint32_t *val, uint32_t V, uint32_t src) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
         val[i] = ALG == kCC ? i : (i == src ? 1u : V + 1u);
-}
-
-// Seeds the first frontier: one vertex, or every vertex (CC, PageRank).
-__global__ void seed_kernel(RegionArgs a, uint32_t src, uint32_t all) {
-    const uint32_t n = all ? a.V : 1;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool won = i < n;
-        const uint32_t v = all ? i : src;
-        if (won) {
-            atomicOr(&a.bitmap[v >> 5], 1u << (v & 31));
-            if (a.visited) atomicOr(&a.visited[v >> 5], 1u << (v & 31));
-        }
-        push_warp(a, won, v);
-    }
 }
 
 // Reached vertices and the sum of their out-degrees (TEPS numerator).
