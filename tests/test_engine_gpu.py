@@ -482,3 +482,19 @@ def test_pinned_result_buffer():
             g.run("bfs", s, out=buf.array)
             assert np.array_equal(buf.array, oracle.bfs(ptr, col, s))
         buf.close()
+
+
+def test_graph_without_edges():
+    """A graph with vertices and no edges: every source reaches only itself."""
+    V = 5
+    ptr = np.zeros(V + 1, np.uint64)
+    with A.Graph.from_csr(ptr, np.zeros(0, np.uint32), budget=A.make_budget(frac=0.25)) as g:
+        got, st = g.run("bfs", 2)
+        assert got.tolist() == [V + 1, V + 1, 1, V + 1, V + 1] and st["reached_edges"] == 0
+        got, _ = g.run("cc")
+        assert got.tolist() == list(range(V))
+        rows, _ = g.run_batch("bfs", [0, 4])
+        assert rows[1].tolist() == [V + 1] * 4 + [1]
+    with A.Graph.from_csr(ptr, np.zeros((0, 2), np.uint32)) as g:
+        got, _ = g.run("sssp", 3)
+        assert got.tolist() == [V + 1, V + 1, V + 1, 1, V + 1]
