@@ -890,6 +890,63 @@ __global__ void __launch_bounds__(kBlock, ASC_PR_MIN_BLOCKS) pr_pull_kernel(PrAr
     if (REF) flush_next(a, s_next);
 }
 
+// Work items of one region for the pull pass (reference mode: its frontier;
+// standard mode: every vertex of the region, long lists as segments).
+template <bool REF>
+__device__ __forceinline__ void pr_items(const RegionArgs &a, uint32_t &n_in, uint32_t &nseg, uint32_t &total,
+                                         bool &bitmap) {
+    bitmap = false;
+    if (REF) {
+        region_items_bits(a, n_in, nseg, total, bitmap);
+    } else {
+        n_in = 0;
+        nseg = a.cnt_in[2 + a.region];
+        total = nseg + (a.dense_end - a.dense_begin + kBlock - 1) / kBlock;
+    }
+}
+
+template <typename T, bool REF>
+__device__ __forceinline__ void pr_item(const PrArgs<T> &p, uint32_t w, uint32_t n_in, uint32_t nseg, bool bitmap,
+                                        PrSmem<T> &sm, uint32_t *s_next) {
+    if (w < nseg) pr_segment<T>(p, p.r.seg_in[w], sm);
+    else if (REF && bitmap) pr_bitmap_tile<T, REF>(p, w - nseg, sm, s_next);
+    else pr_tile<T, REF>(p, w - nseg, n_in, REF ? kList : kRange, sm, s_next);
+}
+
+// Both regions of a pull pass in one launch, items alternating between the
+// on-demand and the static region while both have some (as the traversal's
+// fused expansion), so every SM overlaps host-link reads with HBM reads.
+template <typename T, bool REF>
+__global__ void __launch_bounds__(kBlock, ASC_PR_MIN_BLOCKS) pr_pull_fused_kernel(PrArgs<T> p0, PrArgs<T> p1) {
+    __shared__ PrSmem<T> sm;
+    __shared__ uint32_t s_next[2];
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
+    uint32_t n0, s0, i0, n1, s1, i1;
+    bool b0, b1;
+    pr_items<REF>(p0.r, n0, s0, i0, b0);
+    pr_items<REF>(p1.r, n1, s1, i1, b1);
+    const uint32_t m = min(i0, i1), total = i0 + i1;
+    for (;;) {
+        if (threadIdx.x == 0) sm.work = atomicAdd(p0.r.work, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        __syncthreads();
+        if (w >= total) break;
+        bool od;
+        uint32_t local;
+        if (w < 2 * m) {
+            od = (w & 1) == 0;
+            local = w >> 1;
+        } else {
+            od = i1 > i0;
+            local = m + (w - 2 * m);
+        }
+        if (od) pr_item<T, REF>(p1, local, n1, s1, b1, sm, s_next);
+        else pr_item<T, REF>(p0, local, n0, s0, b0, sm, s_next);
+    }
+    if (REF) flush_next(p0.r, s_next);
+}
+
 // Applies the segmented vertices once all their segments are summed. In
 // reference mode the list is this pass's segment items (k == 0 marks the
 // vertex); in standard mode it is the fixed list of long-list vertices.
@@ -1561,19 +1618,33 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         pa.damping = REF ? 0.85 : p.damping;
         pa.acc = acc + 2 * cp;
         pa.dangling_prev = acc + 2 * (1 - cp) + 1;
+        uint64_t region_items[2];
         for (int region = 0; region < 2; region++) {
-            RegionArgs a = region_args(g, parity, region, !REF);
             const uint32_t range = region == 0 ? g->static_vertices : V - g->static_vertices;
             const bool bitmap_mode = REF && ws->tune.dense_div && cnt[6 + region] > range / ws->tune.dense_div;
             const uint32_t nvert = REF ? (bitmap_mode ? range : cnt[region]) : range;
-            const uint64_t items = (uint64_t)cnt[2 + region] + (nvert + kBlock - 1) / kBlock;
-            if (!items) continue;
-            pa.r = a;
-            ASC_TRY(pt.begin(region));
-            pt.record(s);
-            pr_pull_kernel<T, REF><<<grid_for(ws, items), kBlock, 0, s>>>(pa);
-            pt.record(s);
-            launches++;
+            region_items[region] = (uint64_t)cnt[2 + region] + (nvert + kBlock - 1) / kBlock;
+        }
+        if (!pt.on) {
+            // one launch for both regions (the timed split below runs them apart)
+            if (region_items[0] + region_items[1]) {
+                PrArgs<T> p0 = pa, p1 = pa;
+                p0.r = region_args(g, parity, 0, !REF);
+                p1.r = region_args(g, parity, 1, !REF);
+                pr_pull_fused_kernel<T, REF>
+                    <<<grid_for(ws, region_items[0] + region_items[1]), kBlock, 0, s>>>(p0, p1);
+                launches++;
+            }
+        } else {
+            for (int region = 0; region < 2; region++) {
+                if (!region_items[region]) continue;
+                pa.r = region_args(g, parity, region, !REF);
+                ASC_TRY(pt.begin(region));
+                pt.record(s);
+                pr_pull_kernel<T, REF><<<grid_for(ws, region_items[region]), kBlock, 0, s>>>(pa);
+                pt.record(s);
+                launches++;
+            }
         }
         const uint32_t nseg_items = REF ? cnt[2] + cnt[3] : ws->n_huge_total;
         if (nseg_items) {
