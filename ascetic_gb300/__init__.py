@@ -31,7 +31,7 @@ BFS, SSSP, CC, PR = range(4)
 BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES, BUDGET_MANAGED = range(6)
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
-RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP, RUN_FRAGMENT_COUNTS = 1, 2, 4, 8, 16
+RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP, RUN_FRAGMENT_COUNTS, RUN_GATHER_COPY = 1, 2, 4, 8, 16, 32
 RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 

@@ -73,6 +73,14 @@ struct Workspace {
     uint64_t device_bytes = 0;
     unsigned long long *frag_counts = nullptr;  // per 4096-edge fragment, allocated on first use
     unsigned long long *frag_active = nullptr;  // frag_counts during a counting run, else null
+    // gather-and-copy comparison engine (ASC_RUN_GATHER_COPY), allocated on first use
+    uint32_t *g_stage = nullptr;     // device staging: gathered on-demand edges, edge_words words each
+    uint32_t *g_items = nullptr;     // device: per item (vertex, staged offset, length, first segment)
+    uint32_t *h_stage = nullptr;     // page-locked host staging
+    uint32_t *h_items = nullptr;     // page-locked host items
+    uint32_t *h_list = nullptr;      // page-locked copy of the on-demand frontier list
+    uint64_t *h_segs = nullptr;      // page-locked copy of the on-demand segment items
+    uint64_t g_cap = 0;              // staging capacity in edges (and in items)
 };
 
 }  // namespace asc

@@ -33,6 +33,8 @@
 
 #include <algorithm>
 #include <mutex>
+#include <thread>
+#include <vector>
 #include <string>
 #include <sys/stat.h>
 
@@ -469,6 +471,54 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
         else expand_item<ALG, WORDS>(x.r0, local, n0, s0, m0, sm, s_next);
     }
     flush_next(x.r0, s_next);
+}
+
+// Gather-and-copy comparison engine: expands on-demand edges that host
+// threads gathered into a device staging buffer. Item i is (vertex, offset of
+// its edges in the staging buffer, edge count, 1 for a vertex's first item);
+// a warp takes an item, its lanes 32 edges at a time. Staged edges are plain
+// words (WORDS 1: destination or packed destination/weight) or pairs (2).
+struct StagedArgs {
+    RegionArgs a;
+    const uint32_t *stage;
+    const uint32_t *items;
+    uint32_t n_items;
+};
+
+template <int ALG, int WORDS>
+__global__ void __launch_bounds__(kBlock) expand_staged_kernel(StagedArgs x) {
+    __shared__ uint32_t s_next[2];
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
+    __syncthreads();
+    const RegionArgs &a = x.a;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = warp; i < x.n_items; i += nwarps) {
+        const uint32_t u = x.items[4 * i], off = x.items[4 * i + 1], len = x.items[4 * i + 2];
+        const uint32_t vu = a.val[u];
+        for (uint32_t j0 = 0; j0 < len; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            uint32_t v = 0, nv = 0xffffffffu;
+            if (j < len) {
+                if (WORDS == 2) {
+                    const uint2 e = reinterpret_cast<const uint2 *>(x.stage)[(uint64_t)off + j];
+                    v = e.x;
+                    nv = ALG == kSSSP ? vu + e.y : (ALG == kBFS ? vu + 1 : vu);
+                } else {
+                    const uint32_t e = x.stage[(uint64_t)off + j];
+                    v = e >> a.wbits;
+                    nv = ALG == kBFS ? vu + 1 : (ALG == kSSSP ? vu + (e & ((1u << a.wbits) - 1u)) : vu);
+                }
+            }
+            const uint32_t cur = nv != 0xffffffffu ? probe<ALG>(a, v) : 0;
+            count_next(a, lower<ALG>(a, v, nv, cur), v, s_next);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.stats[1], (unsigned long long)len);
+            if (x.items[4 * i + 3]) atomicAdd(&a.stats[3], 1ull);
+        }
+    }
+    flush_next(a, s_next);
 }
 
 // Builds the next frontier from its bitmap (one thread per 32-vertex word):
@@ -1352,6 +1402,10 @@ void free_ws_buffers(Workspace *ws) {
                     ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
         if (p) cudaFree(p);
     if (ws->h_ctl) cudaFreeHost(ws->h_ctl);
+    for (void *p : {(void *)ws->g_stage, (void *)ws->g_items})
+        if (p) cudaFree(p);
+    for (void *p : {(void *)ws->h_stage, (void *)ws->h_items, (void *)ws->h_list, (void *)ws->h_segs})
+        if (p) cudaFreeHost(p);
     for (auto &e : ws->loop_exec)
         if (e) cudaGraphExecDestroy(e);
     for (auto e : ws->ev)
@@ -1390,9 +1444,125 @@ asc_status run_traversal(asc_graph *g, asc_algo algo, uint32_t source, const asc
         }
         ws->frag_active = ws->frag_counts;
     }
+    // the gather engine expands the on-demand region from its frontier list
+    const uint32_t div = ws->tune.dense_div;
+    if (p.flags & ASC_RUN_GATHER_COPY) ws->tune.dense_div = 0;
     const asc_status rc = run_traversal_impl(g, algo, source, p, out, st);
+    ws->tune.dense_div = div;
     ws->frag_active = nullptr;
     return rc;
+}
+
+typedef void (*StagedFn)(cudaStream_t, const StagedArgs &, uint32_t);
+
+template <int ALG, int WORDS>
+void launch_staged(cudaStream_t s, const StagedArgs &x, uint32_t grid) {
+    expand_staged_kernel<ALG, WORDS><<<grid, kBlock, 0, s>>>(x);
+}
+
+StagedFn pick_staged(asc_algo algo, bool pairs) {
+    if (algo == ASC_BFS) return pairs ? launch_staged<kBFS, 2> : launch_staged<kBFS, 1>;
+    if (algo == ASC_CC) return pairs ? launch_staged<kCC, 2> : launch_staged<kCC, 1>;
+    return pairs ? launch_staged<kSSSP, 2> : launch_staged<kSSSP, 1>;
+}
+
+// Host side of the gather-and-copy engine for one iteration: the on-demand
+// list and segments come back to the host, host threads gather their edges
+// (decoding the stored layout) into page-locked staging in parts of at most
+// g_cap edges, and each part is copied over and expanded before the next.
+asc_status gather_ondemand(asc_graph *g, asc_algo algo, int parity, const uint32_t *cnt, cudaEvent_t lists_ready,
+                           uint32_t &launches) {
+    Workspace *ws = g->ws;
+    cudaStream_t s = g->stream;
+    const uint32_t n_list = cnt[1], n_seg = cnt[3];
+    ASC_CUDA(cudaEventSynchronize(lists_ready));
+    if (!n_list && !n_seg) return ASC_OK;
+    const uint32_t words = g->edge_words;
+    const uint32_t seg_len = ws->tune.segment_edges;
+    struct Item { uint32_t u; uint64_t b; uint32_t len, first; };
+    std::vector<Item> items;
+    items.reserve((size_t)n_list + n_seg);
+    for (uint32_t i = 0; i < n_list; i++) {
+        const uint32_t u = ws->h_list[i];
+        items.push_back({u, g->h_ptr[u], g->h_ptr[u + 1] - g->h_ptr[u], 1u});
+    }
+    for (uint32_t i = 0; i < n_seg; i++) {
+        const uint32_t u = (uint32_t)(ws->h_segs[i] >> 32), k = (uint32_t)ws->h_segs[i];
+        const uint64_t b = (uint64_t)g->h_ptr[u] + (uint64_t)k * seg_len;
+        const uint64_t e = std::min<uint64_t>(g->h_ptr[u + 1], b + seg_len);
+        items.push_back({u, b, (uint32_t)(e - b), k == 0 ? 1u : 0u});
+    }
+    const uint32_t *he = g->h_edges;
+    const uint32_t eb = g->ebits;
+    auto word_at = [&](uint64_t idx) -> uint32_t {
+        if (words == 2 || eb == 32) return he[idx];
+        const uint64_t bit = idx * eb;
+        const uint32_t sh = (uint32_t)(bit & 31);
+        uint32_t x = he[bit >> 5] >> sh;
+        if (sh + eb > 32) x |= he[(bit >> 5) + 1] << (32 - sh);
+        return x & ((1u << eb) - 1u);
+    };
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const StagedFn staged = pick_staged(algo, words == 2);
+    size_t i0 = 0;
+    while (i0 < items.size()) {
+        // one part: items whose edges fit the staging buffer
+        uint64_t tot = 0;
+        size_t i1 = i0;
+        while (i1 < items.size() && i1 - i0 < ws->g_cap && tot + items[i1].len <= ws->g_cap) tot += items[i1++].len;
+        const size_t n = i1 - i0;
+        std::vector<uint64_t> off(n + 1, 0);
+        for (size_t k = 0; k < n; k++) off[k + 1] = off[k] + items[i0 + k].len;
+        auto work = [&](unsigned t) {
+            for (size_t k = t; k < n; k += hw) {
+                const Item &it = items[i0 + k];
+                uint32_t *dst = ws->h_stage + off[k] * words;
+                if (words == 2) memcpy(dst, he + 2 * it.b, 8ull * it.len);
+                else for (uint32_t j = 0; j < it.len; j++) dst[j] = word_at(it.b + j);
+                uint32_t *q = ws->h_items + 4 * k;
+                q[0] = it.u;
+                q[1] = (uint32_t)off[k];
+                q[2] = it.len;
+                q[3] = it.first;
+            }
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < hw; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+        ASC_CUDA(cudaMemcpyAsync(ws->g_stage, ws->h_stage, 4ull * words * tot, cudaMemcpyHostToDevice, s));
+        ASC_CUDA(cudaMemcpyAsync(ws->g_items, ws->h_items, 16ull * n, cudaMemcpyHostToDevice, s));
+        StagedArgs x;
+        x.a = region_args(g, parity, 1, false);
+        attach_far(g, algo, x.a);
+        x.stage = ws->g_stage;
+        x.items = ws->g_items;
+        x.n_items = (uint32_t)n;
+        staged(s, x, fill_grid(ws, 32ull * n));
+        launches++;
+        ASC_CUDA(cudaGetLastError());
+        // the staging buffers are reused by the next part
+        ASC_CUDA(cudaStreamSynchronize(s));
+        i0 = i1;
+    }
+    return ASC_OK;
+}
+
+asc_status ensure_gather_buffers(asc_graph *g) {
+    Workspace *ws = g->ws;
+    if (ws->g_stage) return ASC_OK;
+    const uint64_t od = g->E - std::min<uint64_t>(g->E, g->h_ptr[g->static_vertices]);
+    // a part must hold the longest item: a list up to huge_degree edges or a segment
+    const uint64_t need = std::max<uint64_t>(ws->tune.huge_degree, ws->tune.segment_edges);
+    ws->g_cap = std::max<uint64_t>(need, std::min<uint64_t>(std::max<uint64_t>(od, 1), 1ull << 25));
+    const uint64_t words = g->edge_words;
+    ASC_CUDA(cudaMalloc(&ws->g_stage, 4 * words * ws->g_cap));
+    ASC_CUDA(cudaMalloc(&ws->g_items, 16 * ws->g_cap));
+    ASC_CUDA(cudaHostAlloc(&ws->h_stage, 4 * words * ws->g_cap, cudaHostAllocDefault));
+    ASC_CUDA(cudaHostAlloc(&ws->h_items, 16 * ws->g_cap, cudaHostAllocDefault));
+    ASC_CUDA(cudaHostAlloc(&ws->h_list, 4 * (g->V + 1), cudaHostAllocDefault));
+    ASC_CUDA(cudaHostAlloc(&ws->h_segs, 8 * (ws->segcap_ondemand + 1), cudaHostAllocDefault));
+    return ASC_OK;
 }
 
 asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
@@ -1430,7 +1600,10 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     const int64_t cap = p.max_iterations > 0 ? p.max_iterations : (int64_t)4 * V + 64;
     // fragment counting runs the host-driven loop: the captured graph loop is
     // built without counters
-    const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS));
+    const bool gather = (p.flags & ASC_RUN_GATHER_COPY) != 0;
+    if (gather) ASC_TRY(ensure_gather_buffers(g));
+    const bool use_graph =
+        !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY));
     int iters = 0;
     double phase_ms[2] = {0, 0};
     if (use_graph) {
@@ -1459,7 +1632,23 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         const int po = 1 - parity;
         ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_BLOCK * po, 0, 4 * CTL_BLOCK, s));
         ASC_CUDA(cudaMemsetAsync(ws->bitmap[po], 0, 4 * (V / 32 + 2), s));
-        if (pt.on) {
+        if (gather) {
+            // the on-demand list and segments go to the host first, so the host
+            // gathers while the static region expands on the device
+            ASC_CUDA(cudaMemcpyAsync(ws->h_list, ws->queue[parity] + g->static_vertices, 4ull * cnt[1],
+                                     cudaMemcpyDeviceToHost, s));
+            ASC_CUDA(cudaMemcpyAsync(ws->h_segs, ws->segs[parity] + ws->segcap_static, 8ull * cnt[3],
+                                     cudaMemcpyDeviceToHost, s));
+            ASC_CUDA(cudaEventRecord(ws->ev[3], s));
+            const uint64_t items0 = region_work(0);
+            if (items0) {
+                RegionArgs a = region_args(g, parity, 0, false);
+                attach_far(g, algo, a);
+                expand(g, a, grid_for(ws, items0));
+                launches++;
+            }
+            ASC_TRY(gather_ondemand(g, algo, parity, cnt, ws->ev[3], launches));
+        } else if (pt.on) {
             // diagnostic: one launch per region, each timed on its own
             if (near_far(g, algo)) ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, s));
             for (int region = 0; region < 2; region++) {

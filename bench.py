@@ -71,6 +71,8 @@ def parse():
                     help="host-link rate by run length and the BFS's pattern-limited on-demand ceiling")
     ap.add_argument("--fragment-study", action="store_true",
                     help="edge reads per 4096-edge fragment: what a fragment cache could move off the link")
+    ap.add_argument("--gather-study", action="store_true",
+                    help="the reference's transfer scheme (host gather + copy per iteration) beside zero-copy reads")
     ap.add_argument("--uvm-study", action="store_true",
                     help="compare BFS on the managed-memory (UVM) engine with the split engine")
     return ap.parse_args()
@@ -415,6 +417,46 @@ def _fragment_shares(g):
             "link_bytes_saved_at_best": round((best - prefix) / (1 - prefix), 4) if prefix < 1 else 0.0}
 
 
+def gather_study(args):
+    """What the zero-copy reads buy against the reference's own transfer
+    scheme on the same GPU and budget: every iteration the on-demand frontier
+    goes to the host, host threads gather its edges into page-locked staging,
+    one copy moves them over and a kernel expands them (RUN_GATHER_COPY), as
+    GraphMeta.cuh:469-578 / CalculateOpt.cu:146-178 do (the reference copies
+    from pageable memory, which is slower still)."""
+    import ascetic_gb300 as A
+    A.lib()
+    ptr, col = A.rmat_csr(args.scale, args.edge_factor, args.seed)
+    srcs = pick_sources(ptr, 8, args.seed)
+    out = {"study": "zero-copy on-demand reads vs host gather + copy per iteration (BFS)",
+           "rmat_scale": args.scale, "budget_frac": args.budget, "sources": len(srcs)}
+    # with the bit stream (the engine's layout) and with plain 32-bit words (the
+    # reference's layout, where the host gather is a plain copy per list)
+    for suffix, packing in (("", None), ("_32bit", "0")):
+        if packing is not None:
+            os.environ["ASC_EDGE_PACKING"] = packing
+        with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=args.budget)) as g:
+            for name, flags in (("zero_copy", A.RUN_NO_OUTPUT), ("gather_copy", A.RUN_NO_OUTPUT | A.RUN_GATHER_COPY)):
+                prm = A.make_params(flags=flags)
+                g.run("bfs", srcs[0], params=prm)
+                ms, edges, od = 0.0, 0, 0
+                for s_ in srcs:
+                    _, st = g.run("bfs", s_, params=prm)
+                    ms += st["ms_total"]
+                    edges += st["reached_edges"]
+                    od += st["ondemand_bytes"]
+                out[name + suffix] = {"ms_per_bfs": round(ms / len(srcs), 3),
+                                      "gteps": round(edges / (ms * 1e-3) / 1e9, 2),
+                                      "edge_bits": int(g.info.edge_bits),
+                                      "ondemand_edge_bytes_per_bfs": int(od / len(srcs))}
+        if packing is not None:
+            del os.environ["ASC_EDGE_PACKING"]
+    out["zero_copy_speedup"] = round(out["gather_copy"]["ms_per_bfs"] / out["zero_copy"]["ms_per_bfs"], 2)
+    out["zero_copy_speedup_32bit"] = round(out["gather_copy_32bit"]["ms_per_bfs"] /
+                                           out["zero_copy_32bit"]["ms_per_bfs"], 2)
+    print(json.dumps(out), flush=True)
+
+
 def uvm_study(args):
     """The reference's UVM baseline (edges in managed memory, read-mostly, no
     static region) against the split engine at the same graph and sources:
@@ -499,6 +541,9 @@ def main():
         return
     if args.fragment_study:
         fragment_study(args)
+        return
+    if args.gather_study:
+        gather_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)

@@ -125,9 +125,16 @@ enum {
                                        implies a host-driven iteration loop */
     ASC_RUN_HOST_LOOP = 1u << 3,    /* drive iterations from the host (one readback per iteration)
                                        instead of the CUDA-graph loop */
-    ASC_RUN_FRAGMENT_COUNTS = 1u << 4 /* BFS/SSSP/CC: add the edges this run reads to per-fragment
-                                         counters (4096 edges a fragment; read them with
-                                         asc_graph_fragment_counts); implies ASC_RUN_HOST_LOOP */
+    ASC_RUN_FRAGMENT_COUNTS = 1u << 4, /* BFS/SSSP/CC: add the edges this run reads to per-fragment
+                                          counters (4096 edges a fragment; read them with
+                                          asc_graph_fragment_counts); implies ASC_RUN_HOST_LOOP */
+    ASC_RUN_GATHER_COPY = 1u << 5      /* BFS/SSSP/CC comparison engine, the reference's (and Subway's)
+                                          transfer scheme: every iteration the on-demand frontier list
+                                          goes to the host, host threads gather its edges into a
+                                          page-locked staging buffer, one copy moves them to the
+                                          device and a kernel expands them there (GraphMeta.cuh:469-578,
+                                          CalculateOpt.cu:146-178); the static region runs as usual.
+                                          Same values; implies ASC_RUN_HOST_LOOP */
 };
 
 typedef struct asc_params {

@@ -498,3 +498,28 @@ def test_graph_without_edges():
     with A.Graph.from_csr(ptr, np.zeros((0, 2), np.uint32)) as g:
         got, _ = g.run("sssp", 3)
         assert got.tolist() == [V + 1, V + 1, V + 1, 1, V + 1]
+
+
+@pytest.mark.parametrize("frac", [0.0, 0.3])
+def test_gather_copy_engine_matches(frac):
+    """The gather-and-copy comparison engine (on-demand edges gathered on the
+    host and copied each iteration) gives the same values, for every stored
+    layout: bit stream, packed weighted words, {dst, weight} pairs."""
+    ptr, adj = A.rmat_csr(13, 16, 91, weights=(1, 63))
+    col = adj[:, 0].copy()
+    big = adj.copy()
+    big[:, 1] = (big[:, 1].astype(np.uint64) * 40000).astype(np.uint32)   # too wide to pack: pairs
+    gat = A.make_params(flags=A.RUN_GATHER_COPY)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+        for s in (0, 321):
+            got, st = g.run("bfs", s, params=gat)
+            assert np.array_equal(got, oracle.bfs(ptr, col, s))
+            if frac == 0.0 and st["reached_vertices"] > 1000:
+                assert st["ondemand_edges"] > 0
+        got, _ = g.run("cc", params=gat)
+        assert np.array_equal(got, oracle.cc(ptr, col))
+    for arr in (adj, big):
+        with A.Graph.from_csr(ptr, arr, budget=A.make_budget(frac=frac)) as g:
+            for s in (0, 321):
+                got, _ = g.run("sssp", s, params=gat)
+                assert np.array_equal(got, oracle.sssp(ptr, arr, s))
