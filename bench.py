@@ -721,7 +721,7 @@ def main():
         _, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
         with A.Graph.from_csr(ptr, adj, budget=budget) as gw:
             if not args.no_tune:
-                gw.tune("sssp", tune_srcs[:2], cache=False)
+                gw.tune("sssp", tune_srcs, cache=False)
             gw.run("sssp", srcs[0], params=A.make_params(flags=A.RUN_NO_OUTPUT))
             e, ms, proc, its = 0, 0.0, 0, 0
             for s in srcs[:4]:
