@@ -246,6 +246,8 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
             atomicOr(&a.far_bits[v >> 5], bit);  // waits until the threshold reaches it
             return false;
         }
+        // now near: drop it from the far set, or a later promotion expands it twice
+        if (a.far_bits[v >> 5] & bit) atomicAnd(&a.far_bits[v >> 5], ~bit);
     } else {
         // fire-and-forget: if another thread lowered v further since the probe,
         // it set v's bit too, so the next frontier is the same either way
