@@ -1693,7 +1693,9 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         if (pt.on) ASC_TRY(pt.sum(phase_ms));
         parity = po;
     }
-    if (algo != ASC_CC) {
+    // a BFS expands every reached vertex exactly once, so its expansion counts
+    // already are the reached vertices and edges; SSSP re-expands, so count them
+    if (algo == ASC_SSSP) {
         reached_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(ws->val, g->d_ptr, V,
                                                            (unsigned long long *)(ws->ctl + CTL_STATS) + 4);
         launches++;
@@ -1727,6 +1729,9 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         if (algo == ASC_CC) {
             st->reached_vertices = V;
             st->reached_edges = g->E;
+        } else if (algo == ASC_BFS) {
+            st->reached_vertices = hs[2] + hs[3];
+            st->reached_edges = hs[0] + hs[1];
         } else {
             st->reached_vertices = hs[4];
             st->reached_edges = hs[5];

@@ -77,6 +77,7 @@ def test_bfs_matches_oracle(frac):
                 got, st = g.run("bfs", s, params=A.make_params(flags=flags))
                 assert np.array_equal(got, exp), (frac, s, flags)
                 assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
+                assert st["reached_vertices"] == int((exp != len(ptr)).sum())
                 if g.info.static_edges < g.E and st["reached_vertices"] > 1000:
                     assert st["ondemand_edges"] > 0
                 iters.add(st["iterations"])
