@@ -51,13 +51,13 @@ constexpr unsigned kFull = 0xffffffffu;
 // the warps: the loads over the host link want every warp the SM can hold).
 // The same for the PageRank pull/scatter kernels (8: FP32 standard PageRank on
 // RMAT scale 23 in 181 ms against 195 at the compiler's choice of 40 registers)
-// and the 64-source batch kernels (left to the compiler: at 6 or 8 the batched
-// SSSP kernel spills).
+// The batched SSSP kernel takes 5 (48 registers, no spills; at 6 or 8 it
+// spills); the batched BFS kernels are left to the compiler.
 #ifndef ASC_PR_MIN_BLOCKS
 #define ASC_PR_MIN_BLOCKS 8
 #endif
 #ifndef ASC_MS_MIN_BLOCKS
-#define ASC_MS_MIN_BLOCKS 1
+#define ASC_MS_MIN_BLOCKS 5
 #endif
 #ifndef ASC_EXPAND_MIN_BLOCKS
 #define ASC_EXPAND_MIN_BLOCKS 8
@@ -2115,13 +2115,34 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 // <= 16, 156 at <= 32, 292 always).
 constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
 
+#ifndef ASC_MS_SSSP_ROWS
+#define ASC_MS_SSSP_ROWS 4
+#endif
+// Distance rows a half-warp loads before it compares any of them (the dense
+// path), so the row reads of that many edges are in flight together.
+constexpr int kMsRows = ASC_MS_SSSP_ROWS;
+
 __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs &a, uint32_t u, uint64_t b,
                                               uint32_t n) {
     const int lane = threadIdx.x & 31;
     const unsigned long long f = m.front[u];
-    if (__popcll(f) <= kMsSparseSources) {
+    const int nsrc = __popcll(f);
+    if (nsrc <= kMsSparseSources) {
         // few sources: each lane takes one edge and relaxes it for every active
-        // source, so a warp instruction covers 32 edges instead of one
+        // source, so a warp instruction covers 32 edges instead of one; the
+        // sources' distances at u are read once, and a lane loads its edge's
+        // values for all of them before comparing any
+        uint32_t ds[kMsSparseSources];
+        int sx[kMsSparseSources];
+        {
+            unsigned long long fm = f;
+#pragma unroll
+            for (int k = 0; k < kMsSparseSources; k++) {
+                sx[k] = fm ? __ffsll((long long)fm) - 1 : 0;
+                ds[k] = k < nsrc ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0;
+                fm &= fm - 1;
+            }
+        }
         for (uint32_t c = 0; c < n; c += 32) {
             const bool ok = c + lane < n;
             uint32_t v = 0, w = 0;
@@ -2137,16 +2158,16 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
                 }
             }
             uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+            uint32_t cur[kMsSparseSources];
+#pragma unroll
+            for (int k = 0; k < kMsSparseSources; k++) cur[k] = ok && k < nsrc ? row[sx[k]] : 0u;
             unsigned long long imp = 0;
-            for (unsigned long long fm = f; fm; fm &= fm - 1) {
-                const int s = __ffsll((long long)fm) - 1;
-                const uint32_t ds = m.dist[(uint64_t)u * kMaxBatch + s];
-                if (ok) {
-                    const uint32_t nd = ds + w;
-                    if (nd < row[s]) {
-                        atomicMin(&row[s], nd);  // fire-and-forget, as in the dense path below
-                        imp |= 1ull << s;
-                    }
+#pragma unroll
+            for (int k = 0; k < kMsSparseSources; k++) {
+                const uint32_t nd = ds[k] + w;
+                if (ok && k < nsrc && nd < cur[k]) {
+                    atomicMin(&row[sx[k]], nd);  // fire-and-forget, as in the dense path below
+                    imp |= 1ull << sx[k];
                 }
             }
             if (imp) {
@@ -2158,7 +2179,8 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
     }
     // many sources: each half-warp takes one edge, each of its 16 lanes four
     // sources (one 16-byte load of the destination's distance row per lane),
-    // so a warp relaxes two edges per pass
+    // so a warp relaxes two edges per pass; kMsRows passes load their rows
+    // before any of them is compared
     const uint32_t half = (uint32_t)lane >> 4, l = (uint32_t)lane & 15u;
     const uint4 du = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * kMaxBatch)[l];
     const uint32_t act4 = (uint32_t)(f >> (4 * l)) & 0xfu;
@@ -2176,31 +2198,44 @@ __device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs 
             }
         }
         const uint32_t cn = min(32u, n - c);
-        for (uint32_t j0 = 0; j0 < cn; j0 += 2) {
-            const uint32_t j = j0 + half;
-            const uint32_t v = __shfl_sync(kFull, ev, j & 31), w = __shfl_sync(kFull, ew, j & 31);
-            const bool ok = j < cn;
-            uint32_t imp = 0;
-            if (ok && act4) {
-                uint32_t *row = m.dist + (uint64_t)v * kMaxBatch + 4 * l;
-                const uint4 cur = *reinterpret_cast<const uint4 *>(row);
-                const uint32_t nd0 = du.x + w, nd1 = du.y + w, nd2 = du.z + w, nd3 = du.w + w;
-                // the lowering is fire-and-forget: a source whose value another
-                // thread lowered further in the meantime is marked active for v
-                // all the same, which costs at most a relaxation of v with its
-                // current distance and never changes the fixpoint
-                if ((act4 & 1u) && nd0 < cur.x) { atomicMin(row + 0, nd0); imp |= 1u; }
-                if ((act4 & 2u) && nd1 < cur.y) { atomicMin(row + 1, nd1); imp |= 2u; }
-                if ((act4 & 4u) && nd2 < cur.z) { atomicMin(row + 2, nd2); imp |= 4u; }
-                if ((act4 & 8u) && nd3 < cur.w) { atomicMin(row + 3, nd3); imp |= 8u; }
-            }
-            // the half-warp's improved sources as one 64-bit mask
-            unsigned long long im = (unsigned long long)imp << (4 * l);
+        for (uint32_t j0 = 0; j0 < cn; j0 += 2 * kMsRows) {
+            uint32_t v[kMsRows], w[kMsRows];
+            uint4 cur[kMsRows];
+            bool ok[kMsRows];
 #pragma unroll
-            for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
-            if (l == 0 && ok && im) {
-                atomicOr(&m.next[v], im);
-                atomicOr(&m.touched[v >> 5], 1u << (v & 31));
+            for (int k = 0; k < kMsRows; k++) {
+                const uint32_t j = j0 + 2 * k + half;
+                v[k] = __shfl_sync(kFull, ev, j & 31);
+                w[k] = __shfl_sync(kFull, ew, j & 31);
+                ok[k] = j < cn;
+                cur[k] = make_uint4(0, 0, 0, 0);
+                if (ok[k] && act4)
+                    cur[k] = *reinterpret_cast<const uint4 *>(m.dist + (uint64_t)v[k] * kMaxBatch + 4 * l);
+            }
+#pragma unroll
+            for (int k = 0; k < kMsRows; k++) {
+                uint32_t imp = 0;
+                if (ok[k] && act4) {
+                    uint32_t *row = m.dist + (uint64_t)v[k] * kMaxBatch + 4 * l;
+                    const uint32_t nd0 = du.x + w[k], nd1 = du.y + w[k], nd2 = du.z + w[k], nd3 = du.w + w[k];
+                    // the lowering is fire-and-forget: a source whose value
+                    // another thread lowered further in the meantime (or whose
+                    // loaded value was already stale) is marked active for v all
+                    // the same, which costs at most a relaxation of v with its
+                    // current distance and never changes the fixpoint
+                    if ((act4 & 1u) && nd0 < cur[k].x) { atomicMin(row + 0, nd0); imp |= 1u; }
+                    if ((act4 & 2u) && nd1 < cur[k].y) { atomicMin(row + 1, nd1); imp |= 2u; }
+                    if ((act4 & 4u) && nd2 < cur[k].z) { atomicMin(row + 2, nd2); imp |= 4u; }
+                    if ((act4 & 8u) && nd3 < cur[k].w) { atomicMin(row + 3, nd3); imp |= 8u; }
+                }
+                // the half-warp's improved sources as one 64-bit mask
+                unsigned long long im = (unsigned long long)imp << (4 * l);
+#pragma unroll
+                for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
+                if (l == 0 && ok[k] && im) {
+                    atomicOr(&m.next[v[k]], im);
+                    atomicOr(&m.touched[v[k] >> 5], 1u << (v[k] & 31));
+                }
             }
         }
     }

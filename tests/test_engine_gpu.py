@@ -154,6 +154,11 @@ def test_packed_and_unpacked_weighted_edges():
                 assert np.array_equal(got, oracle.bfs(ptr, arr[:, 0].copy(), s))
             rows, _ = g.run_batch("sssp", [0, 41])
             assert np.array_equal(rows[1], oracle.sssp(ptr, arr, 41))
+            # more sources than the few-source path takes: lanes per source
+            many = [0, 41] + list(range(100, 1400, 100))
+            rows, _ = g.run_batch("sssp", many)
+            for i in (0, 1, 7, len(many) - 1):
+                assert np.array_equal(rows[i], oracle.sssp(ptr, arr, many[i])), (packed, many[i])
 
 
 def test_cc_directed_is_min_ancestor():
