@@ -51,8 +51,9 @@ constexpr unsigned kFull = 0xffffffffu;
 // the warps: the loads over the host link want every warp the SM can hold).
 // The same for the PageRank pull/scatter kernels (8: FP32 standard PageRank on
 // RMAT scale 23 in 181 ms against 195 at the compiler's choice of 40 registers)
-// The batched SSSP kernel takes 5 (48 registers, no spills; at 6 or 8 it
-// spills); the batched BFS kernels are left to the compiler.
+// The batched SSSP kernel takes 5 (47 registers, no spills with two rows in
+// flight per half-warp; at 6 or 8 it spills); the batched BFS kernels are left
+// to the compiler.
 #ifndef ASC_PR_MIN_BLOCKS
 #define ASC_PR_MIN_BLOCKS 8
 #endif
@@ -2102,187 +2103,241 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
     }
 }
 
-// Batched SSSP expansion: one warp per work item (a frontier vertex, or one
-// segment of a long list); lanes are sources (two 32-source halves). Edges are
-// loaded 32 at a time, coalesced, and broadcast with shuffles; the 64
-// distances of a destination are one 256-byte row.
+// Batched SSSP expansion: one CTA per work item (a tile of frontier vertices,
+// or one segment of a long list); the 64 distances of a vertex are one
+// 256-byte row of dist.
 #ifndef ASC_MS_SSSP_SPARSE
 #define ASC_MS_SSSP_SPARSE 8
 #endif
-// A frontier vertex active for at most this many sources relaxes its edges
-// lanes-per-edge (one pass per active source) instead of lanes-per-source
-// (64-source batch on RMAT scale 24: 160 ms never, 142 ms at <= 8, 143 at
-// <= 16, 156 at <= 32, 292 always).
+// An edge whose source vertex is active for at most this many sources is
+// relaxed lane-per-edge (one comparison per active source) instead of
+// lanes-per-source (64-source batch on RMAT scale 24, with one warp per
+// vertex: 160 ms never, 142 ms at <= 8, 143 at <= 16, 156 at <= 32, 292 always).
 constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
 
 #ifndef ASC_MS_SSSP_ROWS
-#define ASC_MS_SSSP_ROWS 4
+#define ASC_MS_SSSP_ROWS 2
 #endif
-// Distance rows a half-warp loads before it compares any of them (the dense
-// path), so the row reads of that many edges are in flight together.
+// Distance rows a half-warp loads before it compares any of them (the
+// many-source path), so the row reads of that many edges are in flight together.
 constexpr int kMsRows = ASC_MS_SSSP_ROWS;
 
-__device__ __forceinline__ void ms_sssp_edges(const MsArgs &m, const RegionArgs &a, uint32_t u, uint64_t b,
-                                              uint32_t n) {
-    const int lane = threadIdx.x & 31;
-    const unsigned long long f = m.front[u];
-    const int nsrc = __popcll(f);
-    if (nsrc <= kMsSparseSources) {
-        // few sources: each lane takes one edge and relaxes it for every active
-        // source, so a warp instruction covers 32 edges instead of one; the
-        // sources' distances at u are read once, and a lane loads its edge's
-        // values for all of them before comparing any
-        uint32_t ds[kMsSparseSources];
-        int sx[kMsSparseSources];
-        {
-            unsigned long long fm = f;
-#pragma unroll
-            for (int k = 0; k < kMsSparseSources; k++) {
-                sx[k] = fm ? __ffsll((long long)fm) - 1 : 0;
-                ds[k] = k < nsrc ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0;
-                fm &= fm - 1;
-            }
-        }
-        for (uint32_t c = 0; c < n; c += 32) {
-            const bool ok = c + lane < n;
-            uint32_t v = 0, w = 0;
-            if (ok) {
-                if (a.wbits) {
-                    const uint32_t e = edge_word(a.edges, b + c + lane, a.ebits);
-                    v = e >> a.wbits;
-                    w = e & ((1u << a.wbits) - 1u);
-                } else {
-                    const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
-                    v = e.x;
-                    w = e.y;
-                }
-            }
-            uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
-            uint32_t cur[kMsSparseSources];
-#pragma unroll
-            for (int k = 0; k < kMsSparseSources; k++) cur[k] = ok && k < nsrc ? row[sx[k]] : 0u;
-            unsigned long long imp = 0;
-#pragma unroll
-            for (int k = 0; k < kMsSparseSources; k++) {
-                const uint32_t nd = ds[k] + w;
-                if (ok && k < nsrc && nd < cur[k]) {
-                    atomicMin(&row[sx[k]], nd);  // fire-and-forget, as in the dense path below
-                    imp |= 1ull << sx[k];
-                }
-            }
-            if (imp) {
-                atomicOr(&m.next[v], imp);
-                atomicOr(&m.touched[v >> 5], 1u << (v & 31));
-            }
-        }
-        return;
-    }
-    // many sources: each half-warp takes one edge, each of its 16 lanes four
-    // sources (one 16-byte load of the destination's distance row per lane),
-    // so a warp relaxes two edges per pass; kMsRows passes load their rows
-    // before any of them is compared
-    const uint32_t half = (uint32_t)lane >> 4, l = (uint32_t)lane & 15u;
-    const uint4 du = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * kMaxBatch)[l];
-    const uint32_t act4 = (uint32_t)(f >> (4 * l)) & 0xfu;
-    for (uint32_t c = 0; c < n; c += 32) {
-        uint32_t ev = 0, ew = 0;
-        if (c + lane < n) {
-            if (a.wbits) {
-                const uint32_t e = edge_word(a.edges, b + c + lane, a.ebits);
-                ev = e >> a.wbits;
-                ew = e & ((1u << a.wbits) - 1u);
-            } else {
-                const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + b + c + lane);
-                ev = e.x;
-                ew = e.y;
-            }
-        }
-        const uint32_t cn = min(32u, n - c);
-        for (uint32_t j0 = 0; j0 < cn; j0 += 2 * kMsRows) {
-            uint32_t v[kMsRows], w[kMsRows];
-            uint4 cur[kMsRows];
-            bool ok[kMsRows];
-#pragma unroll
-            for (int k = 0; k < kMsRows; k++) {
-                const uint32_t j = j0 + 2 * k + half;
-                v[k] = __shfl_sync(kFull, ev, j & 31);
-                w[k] = __shfl_sync(kFull, ew, j & 31);
-                ok[k] = j < cn;
-                cur[k] = make_uint4(0, 0, 0, 0);
-                if (ok[k] && act4)
-                    cur[k] = *reinterpret_cast<const uint4 *>(m.dist + (uint64_t)v[k] * kMaxBatch + 4 * l);
-            }
-#pragma unroll
-            for (int k = 0; k < kMsRows; k++) {
-                uint32_t imp = 0;
-                if (ok[k] && act4) {
-                    uint32_t *row = m.dist + (uint64_t)v[k] * kMaxBatch + 4 * l;
-                    const uint32_t nd0 = du.x + w[k], nd1 = du.y + w[k], nd2 = du.z + w[k], nd3 = du.w + w[k];
-                    // the lowering is fire-and-forget: a source whose value
-                    // another thread lowered further in the meantime (or whose
-                    // loaded value was already stale) is marked active for v all
-                    // the same, which costs at most a relaxation of v with its
-                    // current distance and never changes the fixpoint
-                    if ((act4 & 1u) && nd0 < cur[k].x) { atomicMin(row + 0, nd0); imp |= 1u; }
-                    if ((act4 & 2u) && nd1 < cur[k].y) { atomicMin(row + 1, nd1); imp |= 2u; }
-                    if ((act4 & 4u) && nd2 < cur[k].z) { atomicMin(row + 2, nd2); imp |= 4u; }
-                    if ((act4 & 8u) && nd3 < cur[k].w) { atomicMin(row + 3, nd3); imp |= 8u; }
-                }
-                // the half-warp's improved sources as one 64-bit mask
-                unsigned long long im = (unsigned long long)imp << (4 * l);
-#pragma unroll
-                for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
-                if (l == 0 && ok[k] && im) {
-                    atomicOr(&m.next[v[k]], im);
-                    atomicOr(&m.touched[v[k] >> 5], 1u << (v[k] & 31));
-                }
-            }
-        }
+struct MsSsspSmem {
+    uint32_t pref[kBlock + 1];       // exclusive degree prefix of the tile's vertices
+    uint32_t start[kBlock];          // first edge of each
+    uint32_t vid[kBlock];            // vertex id of each
+    unsigned long long f[kBlock];    // frontier mask of each
+    uint32_t warp[kWarps + 1];
+    uint32_t work;
+    uint32_t dv[kWarps][32];         // per warp: many-source edges of the current chunk
+    uint32_t dw[kWarps][32];
+    uint32_t downer[kWarps][32];
+};
+
+__device__ __forceinline__ void ms_sssp_load_edge(const RegionArgs &a, uint64_t idx, uint32_t &v, uint32_t &w) {
+    if (a.wbits) {
+        const uint32_t e = edge_word(a.edges, idx, a.ebits);
+        v = e >> a.wbits;
+        w = e & ((1u << a.wbits) - 1u);
+    } else {
+        const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + idx);
+        v = e.x;
+        w = e.y;
     }
 }
 
-__device__ __forceinline__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t s, uint32_t local) {
-    const int lane = threadIdx.x & 31;
-    if (local < s) {
-        const uint64_t item = a.seg_in[local];
-        const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
-        const uint64_t b = (uint64_t)a.ptr[u] + (uint64_t)k0 * a.seg_len;
-        const uint64_t e = min((uint64_t)a.ptr[u + 1], b + a.seg_len);
-        ms_sssp_edges(m, a, u, b, (uint32_t)(e - b));
-        if (lane == 0) {
-            atomicAdd(&a.stats[a.region], (unsigned long long)(e - b));
-            if (k0 == 0) atomicAdd(&a.stats[2 + a.region], 1ull);
+// One warp relaxes 32 consecutive edges of the tile's flattened edge range
+// [e0, e0 + 32) ∩ [0, total). An edge whose source vertex is active for at most
+// kMsSparseSources sources is relaxed by its own lane for each of them; the
+// others are gathered into the warp's shared slots and relaxed a half-warp per
+// edge, each of the 16 lanes four sources (one 16-byte load of the
+// destination's 256-byte distance row), kMsRows edges per half-warp in flight.
+__device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs &a, MsSsspSmem &sm, uint32_t e0,
+                                              uint32_t total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t e = e0 + lane;
+    const bool ok = e < total;
+    uint32_t o = 0, v = 0, w = 0;
+    unsigned long long f = 0;
+    if (ok) {
+        int lo = 0, hi = kBlock;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sm.pref[mid] <= e) lo = mid;
+            else hi = mid;
+        }
+        o = (uint32_t)lo;
+        ms_sssp_load_edge(a, (uint64_t)sm.start[o] + (e - sm.pref[o]), v, w);
+        f = sm.f[o];
+    }
+    const int nsrc = __popcll(f);
+    const bool dense = nsrc > kMsSparseSources;
+    if (ok && !dense && nsrc) {
+        // few sources: this lane relaxes its edge for each of them, loading
+        // every value before comparing any
+        const uint32_t u = sm.vid[o];
+        uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+        uint32_t ds[kMsSparseSources], cur[kMsSparseSources];
+        int sx[kMsSparseSources];
+        unsigned long long fm = f;
+#pragma unroll
+        for (int k = 0; k < kMsSparseSources; k++) {
+            sx[k] = fm ? __ffsll((long long)fm) - 1 : 0;
+            fm &= fm - 1;
+            ds[k] = k < nsrc ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0u;
+            cur[k] = k < nsrc ? row[sx[k]] : 0u;
+        }
+        unsigned long long imp = 0;
+#pragma unroll
+        for (int k = 0; k < kMsSparseSources; k++) {
+            const uint32_t nd = ds[k] + w;
+            // fire-and-forget lowering: a source lowered further meanwhile (or
+            // whose loaded value was stale) is marked active for v all the same,
+            // which costs at most one more relaxation and never changes the fixpoint
+            if (k < nsrc && nd < cur[k]) {
+                atomicMin(&row[sx[k]], nd);
+                imp |= 1ull << sx[k];
+            }
+        }
+        if (imp) {
+            atomicOr(&m.next[v], imp);
+            atomicOr(&m.touched[v >> 5], 1u << (v & 31));
+        }
+    }
+    const uint32_t dm = __ballot_sync(kFull, ok && dense);
+    if (!dm) return;
+    if (ok && dense) {
+        const uint32_t r = __popc(dm & ((1u << lane) - 1u));
+        sm.dv[wid][r] = v;
+        sm.dw[wid][r] = w;
+        sm.downer[wid][r] = o;
+    }
+    __syncwarp();
+    const uint32_t nd = __popc(dm);
+    const uint32_t half = (uint32_t)lane >> 4, l = (uint32_t)lane & 15u;
+    for (uint32_t j0 = 0; j0 < nd; j0 += 2 * kMsRows) {
+        uint32_t vk[kMsRows], wk[kMsRows], act[kMsRows];
+        uint4 du[kMsRows], cur[kMsRows];
+#pragma unroll
+        for (int k = 0; k < kMsRows; k++) {
+            const uint32_t j = j0 + 2 * k + half;
+            act[k] = 0;
+            vk[k] = 0;
+            wk[k] = 0;
+            du[k] = make_uint4(0, 0, 0, 0);
+            cur[k] = make_uint4(0, 0, 0, 0);
+            if (j < nd) {
+                const uint32_t ow = sm.downer[wid][j];
+                vk[k] = sm.dv[wid][j];
+                wk[k] = sm.dw[wid][j];
+                act[k] = (uint32_t)(sm.f[ow] >> (4 * l)) & 0xfu;
+                if (act[k]) {
+                    du[k] = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)sm.vid[ow] * kMaxBatch)[l];
+                    cur[k] = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)vk[k] * kMaxBatch)[l];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kMsRows; k++) {
+            const uint32_t j = j0 + 2 * k + half;
+            uint32_t imp = 0;
+            if (act[k]) {
+                uint32_t *row = m.dist + (uint64_t)vk[k] * kMaxBatch + 4 * l;
+                const uint32_t n0 = du[k].x + wk[k], n1 = du[k].y + wk[k], n2 = du[k].z + wk[k], n3 = du[k].w + wk[k];
+                if ((act[k] & 1u) && n0 < cur[k].x) { atomicMin(row + 0, n0); imp |= 1u; }
+                if ((act[k] & 2u) && n1 < cur[k].y) { atomicMin(row + 1, n1); imp |= 2u; }
+                if ((act[k] & 4u) && n2 < cur[k].z) { atomicMin(row + 2, n2); imp |= 4u; }
+                if ((act[k] & 8u) && n3 < cur[k].w) { atomicMin(row + 3, n3); imp |= 8u; }
+            }
+            // the half-warp's improved sources as one 64-bit mask
+            unsigned long long im = (unsigned long long)imp << (4 * l);
+#pragma unroll
+            for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
+            if (l == 0 && j < nd && im) {
+                atomicOr(&m.next[vk[k]], im);
+                atomicOr(&m.touched[vk[k] >> 5], 1u << (vk[k] & 31));
+            }
+        }
+    }
+    __syncwarp();  // the slots are rewritten by the next chunk
+}
+
+// One work item of the batched SSSP: a tile of up to 256 list vertices or one
+// segment of a long list. The tile's edges are walked as one flattened range,
+// 32 per warp per pass, so short lists do not leave lanes idle and every warp
+// has loads in flight.
+__device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, uint32_t n_in, uint32_t nseg,
+                             MsSsspSmem &sm) {
+    bool act = false;
+    uint32_t u = 0, start = 0, deg = 0;
+    unsigned long long f = 0;
+    bool seg = w < nseg;
+    if (seg) {
+        if (threadIdx.x == 0) {
+            const uint64_t item = a.seg_in[w];
+            const uint32_t k0 = (uint32_t)item;
+            u = (uint32_t)(item >> 32);
+            const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
+            const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
+            start = (uint32_t)b;
+            deg = (uint32_t)(min((uint64_t)e0, b + a.seg_len) - b);
+            act = k0 == 0;  // the vertex counts once
+            f = m.front[u];
         }
     } else {
-        const uint32_t u = a.q_in[local - s];
-        const uint32_t b = a.ptr[u], e = a.ptr[u + 1];
-        ms_sssp_edges(m, a, u, b, e - b);
-        if (lane == 0) {
-            atomicAdd(&a.stats[a.region], (unsigned long long)(e - b));
-            atomicAdd(&a.stats[2 + a.region], 1ull);
+        const uint32_t i = (w - nseg) * kBlock + threadIdx.x;
+        if (i < n_in) {
+            u = a.q_in[i];
+            start = a.ptr[u];
+            deg = a.ptr[u + 1] - start;
+            act = true;
+            f = m.front[u];
         }
     }
+    uint32_t total;
+    const uint32_t excl = block_excl_scan(deg, total, sm.warp);
+    sm.pref[threadIdx.x] = excl;
+    sm.start[threadIdx.x] = start;
+    sm.vid[threadIdx.x] = u;
+    sm.f[threadIdx.x] = f;
+    if (threadIdx.x == 0) sm.pref[kBlock] = total;
+    const uint32_t nact = __syncthreads_count(act);
+    for (uint32_t base = 0; base < total; base += kBlock)
+        ms_sssp_chunk(m, a, sm, base + (threadIdx.x & ~31u), total);
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.stats[a.region], (unsigned long long)total);
+        atomicAdd(&a.stats[2 + a.region], (unsigned long long)nact);
+    }
+    __syncthreads();
 }
 
-// Work items are per warp and handed out 8 at a time: [static segments and
-// list vertices][on-demand segments and list vertices]. The SSSP batch always
-// builds lists (its RegionArgs carry dense_div = 0).
+// Work items are per CTA: the static region's segments and list tiles and the
+// on-demand region's, interleaved so link-bound and HBM-bound work overlap.
+// The SSSP batch always builds lists (its RegionArgs carry dense_div = 0).
 __global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_sssp_expand_kernel(MsArgs m) {
-    const uint32_t n0 = m.r0.cnt_in[0], s0 = m.r0.cnt_in[2];
-    const uint32_t n1 = m.r1.cnt_in[1], s1 = m.r1.cnt_in[3];
-    const uint32_t t0 = s0 + n0, total = t0 + s1 + n1;
-    const int lane = threadIdx.x & 31;
+    __shared__ MsSsspSmem sm;
+    uint32_t n0, s0, i0, n1, s1, i1;
+    bool m0, m1;
+    region_items_bits(m.r0, n0, s0, i0, m0);
+    region_items_bits(m.r1, n1, s1, i1, m1);
+    const uint32_t mm = min(i0, i1), total = i0 + i1;
     for (;;) {
-        uint32_t c = 0;
-        if (lane == 0) c = atomicAdd(m.work, 1u);
-        c = __shfl_sync(kFull, c, 0);
-        const uint32_t w0 = c * 8;
-        if (w0 >= total) break;
-        const uint32_t w1 = min(total, w0 + 8);
-        for (uint32_t w = w0; w < w1; w++) {
-            if (w < t0) ms_sssp_item(m, m.r0, s0, w);
-            else ms_sssp_item(m, m.r1, s1, w - t0);
+        if (threadIdx.x == 0) sm.work = atomicAdd(m.work, 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        __syncthreads();
+        if (w >= total) break;
+        bool od;
+        uint32_t local;
+        if (w < 2 * mm) {
+            od = (w & 1) == 0;
+            local = w >> 1;
+        } else {
+            od = i1 > i0;
+            local = mm + (w - 2 * mm);
         }
+        if (od) ms_sssp_item(m, m.r1, local, n1, s1, sm);
+        else ms_sssp_item(m, m.r0, local, n0, s0, sm);
     }
 }
 
