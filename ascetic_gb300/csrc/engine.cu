@@ -2111,9 +2111,11 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 #endif
 // An edge whose source vertex is active for at most this many sources is
 // relaxed lane-per-edge (one comparison per active source) instead of
-// lanes-per-source (64-source batch on RMAT scale 24, with one warp per
-// vertex: 160 ms never, 142 ms at <= 8, 143 at <= 16, 156 at <= 32, 292 always).
+// lanes-per-source (64-source batch on RMAT scale 24: 75 ms at <= 8, 82 at
+// <= 16, 101 at <= 32, 179 always lane-per-edge).
 constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
+// Sources whose values a lane of the few-source path loads before comparing.
+constexpr int kMsGroup = kMsSparseSources < 8 ? kMsSparseSources : 8;
 
 #ifndef ASC_MS_SSSP_ROWS
 #define ASC_MS_SSSP_ROWS 2
@@ -2173,30 +2175,32 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
     const int nsrc = __popcll(f);
     const bool dense = nsrc > kMsSparseSources;
     if (ok && !dense && nsrc) {
-        // few sources: this lane relaxes its edge for each of them, loading
-        // every value before comparing any
+        // few sources: this lane relaxes its edge for each of them, loading the
+        // values of kMsGroup sources before comparing any
         const uint32_t u = sm.vid[o];
         uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
-        uint32_t ds[kMsSparseSources], cur[kMsSparseSources];
-        int sx[kMsSparseSources];
-        unsigned long long fm = f;
+        unsigned long long fm = f, imp = 0;
+        while (fm) {
+            uint32_t ds[kMsGroup], cur[kMsGroup];
+            int sx[kMsGroup];
 #pragma unroll
-        for (int k = 0; k < kMsSparseSources; k++) {
-            sx[k] = fm ? __ffsll((long long)fm) - 1 : 0;
-            fm &= fm - 1;
-            ds[k] = k < nsrc ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0u;
-            cur[k] = k < nsrc ? row[sx[k]] : 0u;
-        }
-        unsigned long long imp = 0;
+            for (int k = 0; k < kMsGroup; k++) {
+                sx[k] = fm ? __ffsll((long long)fm) - 1 : -1;
+                fm &= fm - 1;
+                ds[k] = sx[k] >= 0 ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0u;
+                cur[k] = sx[k] >= 0 ? row[sx[k]] : 0u;
+            }
 #pragma unroll
-        for (int k = 0; k < kMsSparseSources; k++) {
-            const uint32_t nd = ds[k] + w;
-            // fire-and-forget lowering: a source lowered further meanwhile (or
-            // whose loaded value was stale) is marked active for v all the same,
-            // which costs at most one more relaxation and never changes the fixpoint
-            if (k < nsrc && nd < cur[k]) {
-                atomicMin(&row[sx[k]], nd);
-                imp |= 1ull << sx[k];
+            for (int k = 0; k < kMsGroup; k++) {
+                const uint32_t nd = ds[k] + w;
+                // fire-and-forget lowering: a source lowered further meanwhile
+                // (or whose loaded value was stale) is marked active for v all
+                // the same, which costs at most one more relaxation and never
+                // changes the fixpoint
+                if (sx[k] >= 0 && nd < cur[k]) {
+                    atomicMin(&row[sx[k]], nd);
+                    imp |= 1ull << sx[k];
+                }
             }
         }
         if (imp) {
