@@ -2107,12 +2107,15 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 // or one segment of a long list); the 64 distances of a vertex are one
 // 256-byte row of dist.
 #ifndef ASC_MS_SSSP_SPARSE
-#define ASC_MS_SSSP_SPARSE 8
+#define ASC_MS_SSSP_SPARSE 4
 #endif
 // An edge whose source vertex is active for at most this many sources is
-// relaxed lane-per-edge (one comparison per active source) instead of
-// lanes-per-source (64-source batch on RMAT scale 24: 75 ms at <= 8, 82 at
-// <= 16, 101 at <= 32, 179 always lane-per-edge).
+// relaxed lane-per-edge, one 4-byte load per source and row; up to
+// kMsQuadSources lane-per-edge a 16-byte quad of sources at a time; above that
+// a half-warp per edge. 64- and 8-source batches on RMAT scale 24: 4-byte
+// loads up to 8 sources and half-warps above: 75 / 30 ms; quads for 5-8: 75 /
+// 26 ms; quads up to 12 or 16: 79-81 / 26 ms; quads for all above 4: 150 / 26
+// ms; 4-byte loads up to 16, 32 or 64 sources: 82, 101, 179 ms (64 sources).
 constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
 // Sources whose values a lane of the few-source path loads before comparing.
 constexpr int kMsGroup = kMsSparseSources < 8 ? kMsSparseSources : 8;
@@ -2123,6 +2126,17 @@ constexpr int kMsGroup = kMsSparseSources < 8 ? kMsSparseSources : 8;
 // Distance rows a half-warp loads before it compares any of them (the
 // many-source path), so the row reads of that many edges are in flight together.
 constexpr int kMsRows = ASC_MS_SSSP_ROWS;
+#ifndef ASC_MS_SSSP_QUAD_SOURCES
+#define ASC_MS_SSSP_QUAD_SOURCES 8
+#endif
+#ifndef ASC_MS_SSSP_QUADS
+#define ASC_MS_SSSP_QUADS 2
+#endif
+// Edges whose source vertex is active for more than kMsSparseSources and at
+// most kMsQuadSources sources are relaxed lane-per-edge a 16-byte quad of
+// sources at a time (kMsQuads quads in flight); above that a half-warp per edge.
+constexpr int kMsQuadSources = ASC_MS_SSSP_QUAD_SOURCES;
+constexpr int kMsQuads = ASC_MS_SSSP_QUADS;
 
 struct MsSsspSmem {
     uint32_t pref[kBlock + 1];       // exclusive degree prefix of the tile's vertices
@@ -2145,6 +2159,51 @@ __device__ __forceinline__ void ms_sssp_load_edge(const RegionArgs &a, uint64_t 
         const uint2 e = __ldg(reinterpret_cast<const uint2 *>(a.edges) + idx);
         v = e.x;
         w = e.y;
+    }
+}
+
+// Relaxes one edge (u -> v, weight w) for the sources in f, lane-per-edge:
+// the lane reads the two distance rows a 16-byte quad (four sources) at a
+// time, only the quads with an active source, kMsQuads quads in flight.
+__device__ __forceinline__ void ms_sssp_lane_quads(const MsArgs &m, uint32_t u, uint32_t v, uint32_t w,
+                                                   unsigned long long f) {
+    const uint4 *urow = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * kMaxBatch);
+    uint32_t *vrow = m.dist + (uint64_t)v * kMaxBatch;
+    uint32_t qm = 0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) qm |= ((f >> (4 * q)) & 0xfull) ? 1u << q : 0u;
+    unsigned long long imp = 0;
+    while (qm) {
+        int qx[kMsQuads];
+        uint4 du[kMsQuads], cur[kMsQuads];
+#pragma unroll
+        for (int k = 0; k < kMsQuads; k++) {
+            qx[k] = qm ? __ffs(qm) - 1 : -1;
+            qm &= qm - 1;
+            du[k] = make_uint4(0, 0, 0, 0);
+            cur[k] = make_uint4(0, 0, 0, 0);
+            if (qx[k] >= 0) {
+                du[k] = urow[qx[k]];
+                cur[k] = reinterpret_cast<const uint4 *>(vrow)[qx[k]];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kMsQuads; k++) {
+            if (qx[k] < 0) continue;
+            const uint32_t a4 = (uint32_t)(f >> (4 * qx[k])) & 0xfu;
+            uint32_t *r = vrow + 4 * qx[k];
+            const uint32_t n0 = du[k].x + w, n1 = du[k].y + w, n2 = du[k].z + w, n3 = du[k].w + w;
+            uint32_t bits = 0;
+            if ((a4 & 1u) && n0 < cur[k].x) { atomicMin(r + 0, n0); bits |= 1u; }
+            if ((a4 & 2u) && n1 < cur[k].y) { atomicMin(r + 1, n1); bits |= 2u; }
+            if ((a4 & 4u) && n2 < cur[k].z) { atomicMin(r + 2, n2); bits |= 4u; }
+            if ((a4 & 8u) && n3 < cur[k].w) { atomicMin(r + 3, n3); bits |= 8u; }
+            imp |= (unsigned long long)bits << (4 * qx[k]);
+        }
+    }
+    if (imp) {
+        atomicOr(&m.next[v], imp);
+        atomicOr(&m.touched[v >> 5], 1u << (v & 31));
     }
 }
 
@@ -2173,8 +2232,8 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
         f = sm.f[o];
     }
     const int nsrc = __popcll(f);
-    const bool dense = nsrc > kMsSparseSources;
-    if (ok && !dense && nsrc) {
+    const bool dense = nsrc > kMsQuadSources, mid = nsrc > kMsSparseSources && !dense;
+    if (ok && nsrc && nsrc <= kMsSparseSources) {
         // few sources: this lane relaxes its edge for each of them, loading the
         // values of kMsGroup sources before comparing any
         const uint32_t u = sm.vid[o];
@@ -2208,6 +2267,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
             atomicOr(&m.touched[v >> 5], 1u << (v & 31));
         }
     }
+    if (ok && mid) ms_sssp_lane_quads(m, sm.vid[o], v, w, f);
     const uint32_t dm = __ballot_sync(kFull, ok && dense);
     if (!dm) return;
     if (ok && dense) {

@@ -67,6 +67,8 @@ def parse():
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
+    ap.add_argument("--batch-study", action="store_true",
+                    help="only the multi-source legs (BFS and SSSP batches vs single runs), one JSON line")
     ap.add_argument("--link-study", action="store_true",
                     help="host-link rate by run length and the BFS's pattern-limited on-demand ceiling")
     ap.add_argument("--fragment-study", action="store_true",
@@ -533,6 +535,76 @@ def replica_reduce(edges, seconds, world):
     return e.item(), t.item()
 
 
+def batch_bfs_leg(A, g, ptr, args):
+    """One batch of up to 64 BFS sources against the same sources one at a
+    time, and rows of a 4-source batch checked against single runs."""
+    bsrc = pick_sources(ptr, args.batch, args.seed + 100)
+    g.run_batch("bfs", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+    _, bst = g.run_batch("bfs", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+    seq_ms, seq_edges = 0.0, 0
+    for s_ in bsrc:
+        _, st = g.run("bfs", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        seq_ms += st["ms_total"]
+        seq_edges += st["reached_edges"]
+    rows, _ = g.run_batch("bfs", bsrc[:4])
+    exact = all(np.array_equal(rows[i], g.run("bfs", s_)[0]) for i, s_ in enumerate(bsrc[:4]))
+    return {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
+            "sequential_ms": round(seq_ms, 3),
+            "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
+            "batch_gteps": round(seq_edges / (bst["ms_total"] * 1e-3) / 1e9, 3),
+            "ondemand_bytes": bst["ondemand_bytes"], "iterations": bst["iterations"],
+            "rows_checked_bit_exact": 4, "bit_exact": bool(exact)}
+
+
+def batch_sssp_leg(A, ptr, budget, args):
+    """One batch of up to 64 SSSP sources (weights uniform in [1, 63]) against
+    the same sources one at a time; rows of the full batch (its many-source
+    relaxation path) checked against single runs when the rows fit in 8 GB of
+    host memory, else rows of a 4-source batch."""
+    V = len(ptr) - 1
+    _, adjb = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
+    with A.Graph.from_csr(ptr, adjb, budget=budget) as gw:
+        del adjb
+        bsrc = pick_sources(ptr, args.batch, args.seed + 200)
+        gw.run_batch("sssp", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        _, bst = gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        seq_ms = 0.0
+        for s_ in bsrc:
+            _, st = gw.run("sssp", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
+            seq_ms += st["ms_total"]
+        if len(bsrc) * V * 4 <= 8 << 30:
+            rows, _ = gw.run_batch("sssp", bsrc)
+            chk = sorted({0, len(bsrc) // 3, 2 * len(bsrc) // 3, len(bsrc) - 1})
+        else:
+            rows, _ = gw.run_batch("sssp", bsrc[:4])
+            chk = list(range(min(4, len(bsrc))))
+        exact = all(np.array_equal(rows[i], gw.run("sssp", bsrc[i])[0]) for i in chk)
+        del rows
+        return {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
+                "sequential_ms": round(seq_ms, 3),
+                "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
+                "iterations": bst["iterations"], "edges_processed": bst["edges_processed"],
+                "ondemand_bytes": bst["ondemand_bytes"], "rows_checked_bit_exact": chk,
+                "bit_exact": bool(exact)}
+
+
+def batch_study(args):
+    """The multi-source legs alone (no single-source timed steps): a batch of
+    up to 64 BFS sources and one of SSSP sources against the same sources one
+    at a time, on the default graph and budget."""
+    import ascetic_gb300 as A
+    A.lib()
+    ptr, col = A.rmat_csr(args.scale, args.edge_factor, args.seed)
+    budget = A.make_budget(frac=args.budget)
+    out = {"study": "multi-source batches vs the same sources one at a time", "rmat_scale": args.scale,
+           "budget_frac": args.budget}
+    with A.Graph.from_csr(ptr, col, budget=budget) as g:
+        out["batch_bfs"] = batch_bfs_leg(A, g, ptr, args)
+    del col
+    out["batch_sssp"] = batch_sssp_leg(A, ptr, budget, args)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.pr_study:
@@ -549,6 +621,9 @@ def main():
         return
     if args.gather_study:
         gather_study(args)
+        return
+    if args.batch_study:
+        batch_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)
@@ -684,50 +759,10 @@ def main():
                       "generate_s": round(t_gen, 2)},
             "host_wall_ms_per_step": round(1e3 * t_wall / args.steps, 3)}
     if args.batch:
-        # multi-source leg: one batch of up to 64 sources vs the same sources one at a time
-        bsrc = pick_sources(ptr, args.batch, args.seed + 100)
-        g.run_batch("bfs", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
-        _, bst = g.run_batch("bfs", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
-        seq_ms, seq_edges = 0.0, 0
-        for s_ in bsrc:
-            _, st = g.run("bfs", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
-            seq_ms += st["ms_total"]
-            seq_edges += st["reached_edges"]
-        rows, _ = g.run_batch("bfs", bsrc[:4])
-        exact = all(np.array_equal(rows[i], g.run("bfs", s_)[0]) for i, s_ in enumerate(bsrc[:4]))
-        line["batch_bfs"] = {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
-                             "sequential_ms": round(seq_ms, 3),
-                             "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
-                             "batch_gteps": round(seq_edges / (bst["ms_total"] * 1e-3) / 1e9, 3),
-                             "ondemand_bytes": bst["ondemand_bytes"], "iterations": bst["iterations"],
-                             "rows_checked_bit_exact": 4, "bit_exact": bool(exact)}
+        line["batch_bfs"] = batch_bfs_leg(A, g, ptr, args)
     g.close()
     if args.batch and args.batch_sssp:
-        _, adjb = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
-        with A.Graph.from_csr(ptr, adjb, budget=budget) as gw:
-            bsrc = pick_sources(ptr, args.batch, args.seed + 200)
-            gw.run_batch("sssp", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
-            _, bst = gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
-            seq_ms = 0.0
-            for s_ in bsrc:
-                _, st = gw.run("sssp", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
-                seq_ms += st["ms_total"]
-            # rows of the full batch (its many-source relaxation path) when the
-            # 64 rows fit in 8 GB of host memory, else of a 4-source batch
-            if len(bsrc) * V * 4 <= 8 << 30:
-                rows, _ = gw.run_batch("sssp", bsrc)
-                chk = sorted({0, len(bsrc) // 3, 2 * len(bsrc) // 3, len(bsrc) - 1})
-            else:
-                rows, _ = gw.run_batch("sssp", bsrc[:4])
-                chk = list(range(min(4, len(bsrc))))
-            exact = all(np.array_equal(rows[i], gw.run("sssp", bsrc[i])[0]) for i in chk)
-            del rows
-            line["batch_sssp"] = {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
-                                  "sequential_ms": round(seq_ms, 3),
-                                  "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
-                                  "iterations": bst["iterations"], "rows_checked_bit_exact": chk,
-                                  "bit_exact": bool(exact)}
-        del adjb
+        line["batch_sssp"] = batch_sssp_leg(A, ptr, budget, args)
 
     if not args.quick:
         extra = {}
