@@ -2112,7 +2112,8 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 // An edge whose source vertex is active for at most this many sources is
 // relaxed lane-per-edge, one 4-byte load per source and row; up to
 // kMsQuadSources lane-per-edge a 16-byte quad of sources at a time; above that
-// a half-warp per edge. 64- and 8-source batches on RMAT scale 24: 4-byte
+// a group of lanes per edge. 64- and 8-source batches on RMAT scale 24 (16 lanes
+// per many-source edge): 4-byte
 // loads up to 8 sources and half-warps above: 75 / 30 ms; quads for 5-8: 75 /
 // 26 ms; quads up to 12 or 16: 79-81 / 26 ms; quads for all above 4: 150 / 26
 // ms; 4-byte loads up to 16, 32 or 64 sources: 82, 101, 179 ms (64 sources).
@@ -2123,8 +2124,8 @@ constexpr int kMsGroup = kMsSparseSources < 8 ? kMsSparseSources : 8;
 #ifndef ASC_MS_SSSP_ROWS
 #define ASC_MS_SSSP_ROWS 2
 #endif
-// Distance rows a half-warp loads before it compares any of them (the
-// many-source path), so the row reads of that many edges are in flight together.
+// Edges a lane group of the many-source path loads the distance rows of before
+// it compares any of them, so those row reads are in flight together.
 constexpr int kMsRows = ASC_MS_SSSP_ROWS;
 #ifndef ASC_MS_SSSP_QUAD_SOURCES
 #define ASC_MS_SSSP_QUAD_SOURCES 8
@@ -2134,9 +2135,19 @@ constexpr int kMsRows = ASC_MS_SSSP_ROWS;
 #endif
 // Edges whose source vertex is active for more than kMsSparseSources and at
 // most kMsQuadSources sources are relaxed lane-per-edge a 16-byte quad of
-// sources at a time (kMsQuads quads in flight); above that a half-warp per edge.
+// sources at a time (kMsQuads quads in flight); above that a lane group per edge.
 constexpr int kMsQuadSources = ASC_MS_SSSP_QUAD_SOURCES;
 constexpr int kMsQuads = ASC_MS_SSSP_QUADS;
+#ifndef ASC_MS_SSSP_LANES
+#define ASC_MS_SSSP_LANES 8
+#endif
+// Lanes that share one many-source edge (16: four sources and one 16-byte
+// load per lane; 8: eight sources and two loads per lane; 4: sixteen and
+// four). 64-source batch on RMAT scale 24: 76 ms at 16 lanes (two edges per
+// group in flight), 69 at 8 (two in flight), 71 at 8 (one), 71 at 4 (one).
+constexpr int kMsLanes = ASC_MS_SSSP_LANES;
+constexpr int kMsPerLane = kMaxBatch / kMsLanes;
+static_assert(kMsLanes == 4 || kMsLanes == 8 || kMsLanes == 16, "4, 8 or 16 lanes per many-source edge");
 
 struct MsSsspSmem {
     uint32_t pref[kBlock + 1];       // exclusive degree prefix of the tile's vertices
@@ -2209,10 +2220,11 @@ __device__ __forceinline__ void ms_sssp_lane_quads(const MsArgs &m, uint32_t u, 
 
 // One warp relaxes 32 consecutive edges of the tile's flattened edge range
 // [e0, e0 + 32) ∩ [0, total). An edge whose source vertex is active for at most
-// kMsSparseSources sources is relaxed by its own lane for each of them; the
-// others are gathered into the warp's shared slots and relaxed a half-warp per
-// edge, each of the 16 lanes four sources (one 16-byte load of the
-// destination's 256-byte distance row), kMsRows edges per half-warp in flight.
+// kMsQuadSources sources is relaxed by its own lane for each of them; the
+// others are gathered into the warp's shared slots and relaxed by groups of
+// kMsLanes lanes, each lane kMsPerLane sources (16-byte loads of the source's
+// and the destination's 256-byte distance rows), kMsRows edges per group in
+// flight.
 __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs &a, MsSsspSmem &sm, uint32_t e0,
                                               uint32_t total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -2278,45 +2290,61 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
     }
     __syncwarp();
     const uint32_t nd = __popc(dm);
-    const uint32_t half = (uint32_t)lane >> 4, l = (uint32_t)lane & 15u;
-    for (uint32_t j0 = 0; j0 < nd; j0 += 2 * kMsRows) {
+    // kMsLanes lanes per edge, kMsPerLane sources (kMsPerLane / 4 quads) per lane
+    constexpr int G = kMsLanes, S = kMsPerLane, Q = kMsPerLane / 4, EPW = 32 / kMsLanes;
+    const uint32_t grp = (uint32_t)lane / G, l = (uint32_t)lane % G;
+    for (uint32_t j0 = 0; j0 < nd; j0 += EPW * kMsRows) {
         uint32_t vk[kMsRows], wk[kMsRows], act[kMsRows];
-        uint4 du[kMsRows], cur[kMsRows];
+        uint4 du[kMsRows][Q], cur[kMsRows][Q];
 #pragma unroll
         for (int k = 0; k < kMsRows; k++) {
-            const uint32_t j = j0 + 2 * k + half;
+            const uint32_t j = j0 + EPW * k + grp;
             act[k] = 0;
             vk[k] = 0;
             wk[k] = 0;
-            du[k] = make_uint4(0, 0, 0, 0);
-            cur[k] = make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                du[k][q] = make_uint4(0, 0, 0, 0);
+                cur[k][q] = make_uint4(0, 0, 0, 0);
+            }
             if (j < nd) {
                 const uint32_t ow = sm.downer[wid][j];
                 vk[k] = sm.dv[wid][j];
                 wk[k] = sm.dw[wid][j];
-                act[k] = (uint32_t)(sm.f[ow] >> (4 * l)) & 0xfu;
+                act[k] = (uint32_t)(sm.f[ow] >> (S * l)) & (uint32_t)((1ull << S) - 1);
                 if (act[k]) {
-                    du[k] = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)sm.vid[ow] * kMaxBatch)[l];
-                    cur[k] = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)vk[k] * kMaxBatch)[l];
+                    const uint4 *ur = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)sm.vid[ow] * kMaxBatch);
+                    const uint4 *vr = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)vk[k] * kMaxBatch);
+#pragma unroll
+                    for (int q = 0; q < Q; q++) {
+                        du[k][q] = ur[Q * l + q];
+                        cur[k][q] = vr[Q * l + q];
+                    }
                 }
             }
         }
 #pragma unroll
         for (int k = 0; k < kMsRows; k++) {
-            const uint32_t j = j0 + 2 * k + half;
+            const uint32_t j = j0 + EPW * k + grp;
             uint32_t imp = 0;
             if (act[k]) {
-                uint32_t *row = m.dist + (uint64_t)vk[k] * kMaxBatch + 4 * l;
-                const uint32_t n0 = du[k].x + wk[k], n1 = du[k].y + wk[k], n2 = du[k].z + wk[k], n3 = du[k].w + wk[k];
-                if ((act[k] & 1u) && n0 < cur[k].x) { atomicMin(row + 0, n0); imp |= 1u; }
-                if ((act[k] & 2u) && n1 < cur[k].y) { atomicMin(row + 1, n1); imp |= 2u; }
-                if ((act[k] & 4u) && n2 < cur[k].z) { atomicMin(row + 2, n2); imp |= 4u; }
-                if ((act[k] & 8u) && n3 < cur[k].w) { atomicMin(row + 3, n3); imp |= 8u; }
-            }
-            // the half-warp's improved sources as one 64-bit mask
-            unsigned long long im = (unsigned long long)imp << (4 * l);
+                uint32_t *row = m.dist + (uint64_t)vk[k] * kMaxBatch + S * l;
 #pragma unroll
-            for (int d = 8; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
+                for (int q = 0; q < Q; q++) {
+                    const uint32_t n0 = du[k][q].x + wk[k], n1 = du[k][q].y + wk[k];
+                    const uint32_t n2 = du[k][q].z + wk[k], n3 = du[k][q].w + wk[k];
+                    const uint32_t a4 = act[k] >> (4 * q);
+                    uint32_t *r = row + 4 * q;
+                    if ((a4 & 1u) && n0 < cur[k][q].x) { atomicMin(r + 0, n0); imp |= 1u << (4 * q); }
+                    if ((a4 & 2u) && n1 < cur[k][q].y) { atomicMin(r + 1, n1); imp |= 2u << (4 * q); }
+                    if ((a4 & 4u) && n2 < cur[k][q].z) { atomicMin(r + 2, n2); imp |= 4u << (4 * q); }
+                    if ((a4 & 8u) && n3 < cur[k][q].w) { atomicMin(r + 3, n3); imp |= 8u << (4 * q); }
+                }
+            }
+            // the group's improved sources as one 64-bit mask
+            unsigned long long im = (unsigned long long)imp << (S * l);
+#pragma unroll
+            for (int d = G / 2; d > 0; d >>= 1) im |= __shfl_xor_sync(kFull, im, d);
             if (l == 0 && j < nd && im) {
                 atomicOr(&m.next[vk[k]], im);
                 atomicOr(&m.touched[vk[k] >> 5], 1u << (vk[k] & 31));

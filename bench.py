@@ -566,7 +566,8 @@ def batch_sssp_leg(A, ptr, budget, args):
     with A.Graph.from_csr(ptr, adjb, budget=budget) as gw:
         del adjb
         bsrc = pick_sources(ptr, args.batch, args.seed + 200)
-        gw.run_batch("sssp", bsrc[:2], params=A.make_params(flags=A.RUN_NO_OUTPUT))
+        # warm-up: the same batch once (its launches are the ones to profile)
+        gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
         _, bst = gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
         seq_ms = 0.0
         for s_ in bsrc:
