@@ -223,18 +223,29 @@ __device__ __forceinline__ uint32_t probe(const RegionArgs &a, uint32_t v) {
     return ALG == kBFS ? a.visited[v >> 5] : a.val[v];
 }
 
-// Lowers val[v] to nv; true when this thread also won v's next-frontier bit.
+#ifndef ASC_CLAIM_RED
+#define ASC_CLAIM_RED 1
+#endif
+// Lowers val[v] to nv; true when this thread counts v into the next frontier.
 // cur is the earlier probe: reached bits and values only ever grow / shrink,
 // so a stale probe can only cost an extra atomic, never a missed update.
 // BFS is level-synchronous: every update of an iteration writes the same
-// level, so the first thread to set v's reached bit stores it and no atomicMin
+// level, so a thread whose probe found v unreached stores it and no atomicMin
 // is needed (the result equals the atomicMin relaxation's fixpoint).
+// With kClaimRed the atomics are fire-and-forget (no thread waits for a
+// returned old value): two threads with stale probes may both store v's level
+// (the same value) and both count v, so the per-region next-frontier counts
+// are upper bounds. They only choose between list and bitmap walks and stop
+// the loop when zero, which stays exact: a count is zero only when no thread
+// set a bit. Otherwise the returned old bit decides, and counts are exact.
+constexpr bool kClaimRed = ASC_CLAIM_RED != 0;
 template <int ALG>
 __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t nv, uint32_t cur) {
     const uint32_t bit = 1u << (v & 31);
     if (ALG == kBFS) {
         if (nv == 0xffffffffu || (cur & bit)) return false;
-        if (atomicOr(&a.visited[v >> 5], bit) & bit) return false;
+        if (kClaimRed) atomicOr(&a.visited[v >> 5], bit);
+        else if (atomicOr(&a.visited[v >> 5], bit) & bit) return false;
         a.val[v] = nv;
         atomicOr(&a.bitmap[v >> 5], bit);
         return true;
@@ -253,6 +264,10 @@ __device__ __forceinline__ bool lower(const RegionArgs &a, uint32_t v, uint32_t 
         // fire-and-forget: if another thread lowered v further since the probe,
         // it set v's bit too, so the next frontier is the same either way
         atomicMin(&a.val[v], nv);
+    }
+    if (kClaimRed) {
+        atomicOr(&a.bitmap[v >> 5], bit);
+        return true;
     }
     return (atomicOr(&a.bitmap[v >> 5], bit) & bit) == 0;
 }
