@@ -2528,14 +2528,35 @@ struct Admit {
 // columns.
 __global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint32_t stride, uint32_t **planes,
                                 unsigned long long newmask, uint32_t V, uint32_t fill, uint32_t sssp) {
+    if (sssp) {
+        // a half-warp per distance row (stride 64): lane l owns sources
+        // 4l..4l+3, one 16-byte store when all four are new, else a merge
+        const uint32_t l = threadIdx.x & 15u;
+        const uint32_t m4 = (uint32_t)(newmask >> (4 * l)) & 0xfu;
+        if (!m4) return;
+        const uint64_t h0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+        const uint64_t hs = ((uint64_t)gridDim.x * blockDim.x) >> 4;
+        for (uint64_t v = h0; v < V; v += hs) {
+            uint4 *p = reinterpret_cast<uint4 *>(dist + v * stride) + l;
+            uint4 x = make_uint4(fill, fill, fill, fill);
+            if (m4 != 0xfu) {
+                const uint4 o = *p;
+                if (!(m4 & 1u)) x.x = o.x;
+                if (!(m4 & 2u)) x.y = o.y;
+                if (!(m4 & 4u)) x.z = o.z;
+                if (!(m4 & 8u)) x.w = o.w;
+            }
+            *p = x;
+        }
+        return;
+    }
     for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
         unsigned long long t = newmask;
-        if (!sssp) visit[v] &= ~newmask;
+        visit[v] &= ~newmask;
         while (t) {
             const int s = __ffsll((long long)t) - 1;
             t &= t - 1;
-            if (sssp) dist[v * stride + s] = fill;
-            else planes[s][v] = fill;
+            planes[s][v] = fill;
         }
     }
 }
