@@ -67,6 +67,8 @@ def parse():
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
+    ap.add_argument("--budget-study", action="store_true",
+                    help="BFS GTEPS by static fraction of edge bytes (all in HBM down to all on demand)")
     ap.add_argument("--batch-study", action="store_true",
                     help="only the multi-source legs (BFS and SSSP batches vs single runs), one JSON line")
     ap.add_argument("--link-study", action="store_true",
@@ -212,6 +214,18 @@ def pr_study(args):
                      "max_abs_err_vs_fp64_oracle": float(np.abs(r - exact).max()),
                      "l1_err_vs_fp64_oracle": float(np.abs(r - exact).sum()),
                      "ondemand_bytes": st["ondemand_bytes"]}
+    # FP32 pass time against the static fraction: every edge in HBM (the pull's
+    # random rank gathers alone), the 30% budget, every edge read on demand
+    by_budget = {}
+    for frac in (1.0, 0.30, 0.0):
+        with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=frac)) as g:
+            prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32, flags=A.RUN_NO_OUTPUT)
+            g.run("pr", params=prm)
+            _, st = g.run("pr", params=prm)
+            by_budget[str(frac)] = {"ms_per_pass": round(st["ms_total"] / st["iterations"], 3),
+                                    "ondemand_gb_per_pass": round(st["ondemand_bytes"] / st["iterations"] / 1e9, 4),
+                                    "ondemand_gbps": round(st["ondemand_bytes"] / (st["ms_total"] * 1e-3) / 1e9, 1)}
+    out["fp32_pass_by_budget"] = by_budget
     out["fp32_vs_fp64_gpu_max_abs"] = float(np.abs(res["fp32"][0] - res["fp64"][0]).max())
     out["oracle"] = {"passes": it, "residual": resid, "seconds_1_core": round(oracle_s, 1)}
     out["within_1e-6"] = bool(out["fp32"]["max_abs_err_vs_fp64_oracle"] <= 1e-6)
@@ -464,6 +478,37 @@ def gather_study(args):
     print(json.dumps(out), flush=True)
 
 
+def budget_study(args):
+    """BFS throughput against the static fraction of the edge bytes, from every
+    edge in HBM to every edge read on demand, same graph and sources, thresholds
+    autotuned per budget on other sources."""
+    import ascetic_gb300 as A
+    A.lib()
+    ptr, col = A.rmat_csr(args.scale, args.edge_factor, args.seed)
+    srcs = pick_sources(ptr, 8, args.seed)
+    tune_srcs = pick_sources(ptr, 4, args.seed + 1000)
+    out = {"study": "BFS GTEPS by static fraction of edge bytes", "rmat_scale": args.scale, "sources": len(srcs),
+           "rows": []}
+    for frac in (1.0, 0.75, 0.5, 0.25, 0.1, 0.0):
+        with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
+            if not args.no_tune:
+                g.tune("bfs", tune_srcs, cache=False)
+            prm = A.make_params(flags=A.RUN_NO_OUTPUT)
+            for s_ in srcs[:3]:
+                g.run("bfs", s_, params=prm)
+            ms, edges, od = 0.0, 0, 0
+            for s_ in srcs:
+                _, st = g.run("bfs", s_, params=prm)
+                ms += st["ms_total"]
+                edges += st["reached_edges"]
+                od += st["ondemand_bytes"]
+            out["rows"].append({"budget_frac": frac, "static_edge_share": round(g.info.static_edges / g.E, 4),
+                                "gteps": round(edges / (ms * 1e-3) / 1e9, 2), "ms_per_bfs": round(ms / len(srcs), 3),
+                                "ondemand_bytes_per_bfs": int(od / len(srcs)),
+                                "ondemand_gbps": round(od / (ms * 1e-3) / 1e9, 1)})
+    print(json.dumps(out), flush=True)
+
+
 def uvm_study(args):
     """The reference's UVM baseline (edges in managed memory, read-mostly, no
     static region) against the split engine at the same graph and sources:
@@ -626,6 +671,9 @@ def main():
         return
     if args.batch_study:
         batch_study(args)
+        return
+    if args.budget_study:
+        budget_study(args)
         return
     if args.impl == "reference":
         reference_arm(args)
