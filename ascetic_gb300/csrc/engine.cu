@@ -50,10 +50,9 @@ constexpr unsigned kFull = 0xffffffffu;
 // bit-packed edges: 65.6 GTEPS at 8, 64.5 at 6, 57.3 at 4 (64 registers, half
 // the warps: the loads over the host link want every warp the SM can hold).
 // The same for the PageRank pull/scatter kernels (8: FP32 standard PageRank on
-// RMAT scale 23 in 181 ms against 195 at the compiler's choice of 40 registers)
-// The batched SSSP kernel takes 5 (47 registers, no spills with two rows in
-// flight per half-warp; at 6 or 8 it spills); the batched BFS kernels are left
-// to the compiler.
+// RMAT scale 23 in 181 ms against 195 at the compiler's choice of 40 registers).
+// The batched SSSP kernel takes 5 (48 registers; at 6 or 8 it spills more than
+// a few bytes); the batched BFS kernels are left to the compiler (32 registers).
 #ifndef ASC_PR_MIN_BLOCKS
 #define ASC_PR_MIN_BLOCKS 8
 #endif
