@@ -169,3 +169,20 @@ def test_bench_replicas_gloo_world2():
         assert p.exitcode == 0
     assert [r[:4] for r in res] == [(0, 2, 3000.0, 1.5), (1, 2, 3000.0, 1.5)]
     assert [r[4] for r in res] == ["4", "5"]   # one device per replica, by local rank
+
+
+def test_bench_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` runs the reference's frontier/atomic-min
+    scheme on the host cores (no GPU) and prints one JSON line with the
+    reference-arm keys."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "12",
+                        "--steps", "2", "--warmup", "1"], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "GTEPS" and line["value"] > 0
+    assert line["steps"] == 2 and line["warmup"] == 1 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert line["config"]["scale"] == 12
