@@ -120,12 +120,17 @@ def test_batch_bfs_rows_equal_single_source(frac):
         assert np.array_equal(one[0], got[3])
 
 
+@pytest.mark.parametrize("n_src", [3, 6, 40])
 @pytest.mark.parametrize("frac", [1.0, 0.25, 0.0])
-def test_batch_sssp_rows_equal_single_source(frac):
+def test_batch_sssp_rows_equal_single_source(frac, n_src):
+    """Rows of a batched SSSP equal single-source runs: 3 sources take the
+    per-source loads, 6 the 16-byte quads, 40 (+3) the lane groups per edge."""
     ptr, adj = A.rmat_csr(12, 16, 32, weights=(1, 63))
     deg = np.diff(ptr)
     rng = np.random.default_rng(6)
-    srcs = rng.choice(np.nonzero(deg)[0], size=40, replace=False).tolist() + [7, 7, int(np.nonzero(deg == 0)[0][0])]
+    srcs = rng.choice(np.nonzero(deg)[0], size=n_src, replace=False).tolist()
+    if n_src > 8:
+        srcs += [7, 7, int(np.nonzero(deg == 0)[0][0])]
     with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=frac)) as g:
         got, st = g.run_batch("sssp", srcs)
         for i, s in enumerate(srcs):
