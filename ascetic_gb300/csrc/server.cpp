@@ -89,6 +89,8 @@ uint64_t budget_left(asc_server *s) {
     return s->cfg.device_budget_bytes > s->used_bytes ? s->cfg.device_budget_bytes - s->used_bytes : 0;
 }
 
+constexpr size_t kLatencyWindow = size_t(1) << 20;
+
 void finish(asc_server *s, Query *q, asc_status st) {
     q->status = st;
     q->state = Q_DONE;
@@ -96,6 +98,9 @@ void finish(asc_server *s, Query *q, asc_status st) {
     s->last_done = q->t_end;
     if (st == ASC_OK) {
         s->completed++;
+        // latencies of the most recent kLatencyWindow completions (a server that
+        // runs for long does not grow without bound)
+        if (s->lat_ms.size() >= kLatencyWindow) s->lat_ms.erase(s->lat_ms.begin(), s->lat_ms.begin() + kLatencyWindow / 2);
         s->lat_ms.push_back(std::chrono::duration<double, std::milli>(q->t_end - q->t_submit).count());
     } else if (st == ASC_ERR_CANCELLED) {
         s->cancelled++;
@@ -445,6 +450,7 @@ asc_status asc_server_submit(asc_server *s, uint32_t graph_id, asc_algo algo, ui
     if (!s || !ticket) return fail(ASC_ERR_INVALID, "asc_server_submit: null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     if (graph_id >= s->graphs.size()) return fail(ASC_ERR_INVALID, "unknown graph %u", graph_id);
+    if ((unsigned)algo > (unsigned)ASC_PR) return fail(ASC_ERR_INVALID, "unknown algorithm");
     asc_graph *g = s->graphs[graph_id].g;
     if ((algo == ASC_BFS || algo == ASC_SSSP) && source >= g->V)
         return fail(ASC_ERR_INVALID, "source %u is not a vertex", source);
@@ -452,7 +458,6 @@ asc_status asc_server_submit(asc_server *s, uint32_t graph_id, asc_algo algo, ui
         return fail(ASC_ERR_UNSUPPORTED, "SSSP needs a weighted graph");
     if ((algo == ASC_BFS || algo == ASC_SSSP || algo == ASC_CC) && g->is_csc)
         return fail(ASC_ERR_UNSUPPORTED, "BFS/SSSP/CC need an out-edge graph");
-    if (algo > ASC_PR) return fail(ASC_ERR_INVALID, "unknown algorithm");
     if (s->queries.size() >= s->cfg.queue_capacity) return fail(ASC_ERR_BUSY, "server queue is full");
     Query *q = new Query();
     q->ticket = s->next_ticket++;

@@ -285,7 +285,7 @@ typedef struct asc_server_stats {
     uint64_t submitted, completed, failed, cancelled;
     uint64_t batch_iterations;
     uint64_t device_bytes;  /* device bytes accounted against the budget */
-    double p50_ms, p99_ms, mean_ms, max_ms;  /* completed-query latency */
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* completed-query latency (the most recent 2^19..2^20) */
     double queries_per_s;   /* completed / (last completion - first submit) */
     double span_s;
 } asc_server_stats;
