@@ -143,6 +143,8 @@ void batch_destroy(BatchEngine *b);
 bool batch_has_plane(BatchEngine *b, uint32_t slot);
 asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source);
 bool batch_busy(const BatchEngine *b);
+// Source slots of a batch: 64, or the row width of a narrower SSSP batch.
+uint32_t batch_slots(const BatchEngine *b);
 asc_status batch_launch(BatchEngine *b);
 asc_status batch_collect(BatchEngine *b, uint64_t *finished);
 asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *out, bool device_out);

@@ -2152,16 +2152,20 @@ constexpr int kMsRows = ASC_MS_SSSP_ROWS;
 // sources at a time (kMsQuads quads in flight); above that a lane group per edge.
 constexpr int kMsQuadSources = ASC_MS_SSSP_QUAD_SOURCES;
 constexpr int kMsQuads = ASC_MS_SSSP_QUADS;
-#ifndef ASC_MS_SSSP_LANES
-#define ASC_MS_SSSP_LANES 8
+#ifndef ASC_MS_SSSP_PER_LANE
+#define ASC_MS_SSSP_PER_LANE 8
 #endif
-// Lanes that share one many-source edge (16: four sources and one 16-byte
-// load per lane; 8: eight sources and two loads per lane; 4: sixteen and
-// four). 64-source batch on RMAT scale 24: 76 ms at 16 lanes (two edges per
-// group in flight), 69 at 8 (two in flight), 71 at 8 (one), 71 at 4 (one).
-constexpr int kMsLanes = ASC_MS_SSSP_LANES;
-constexpr int kMsPerLane = kMaxBatch / kMsLanes;
-static_assert(kMsLanes == 4 || kMsLanes == 8 || kMsLanes == 16, "4, 8 or 16 lanes per many-source edge");
+// Sources per lane of a many-source edge; the lanes sharing the edge are the
+// row width over this (4: one 16-byte load per lane, 16 lanes for a 64-source
+// row; 8: two loads, 8 lanes; 16: four loads, 4 lanes). 64-source batch on RMAT
+// scale 24: 76 ms at 4 per lane (two edges per group in flight), 69 at 8 (two
+// in flight), 71 at 8 (one), 71 at 16 (one).
+constexpr int kMsPerLane = ASC_MS_SSSP_PER_LANE;
+static_assert(kMsPerLane == 4 || kMsPerLane == 8 || kMsPerLane == 16, "4, 8 or 16 sources per lane");
+// Distance rows of a batch hold R = 16, 32 or 64 sources (R x 4 bytes per
+// vertex): the 64-wide batch, or a narrower one where a device budget cannot
+// hold 64 columns of a large graph.
+__host__ __device__ constexpr bool ms_row_ok(int R) { return R == 16 || R == 32 || R == 64; }
 
 struct MsSsspSmem {
     uint32_t pref[kBlock + 1];       // exclusive degree prefix of the tile's vertices
@@ -2190,13 +2194,14 @@ __device__ __forceinline__ void ms_sssp_load_edge(const RegionArgs &a, uint64_t 
 // Relaxes one edge (u -> v, weight w) for the sources in f, lane-per-edge:
 // the lane reads the two distance rows a 16-byte quad (four sources) at a
 // time, only the quads with an active source, kMsQuads quads in flight.
+template <int R>
 __device__ __forceinline__ void ms_sssp_lane_quads(const MsArgs &m, uint32_t u, uint32_t v, uint32_t w,
                                                    unsigned long long f) {
-    const uint4 *urow = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * kMaxBatch);
-    uint32_t *vrow = m.dist + (uint64_t)v * kMaxBatch;
+    const uint4 *urow = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)u * R);
+    uint32_t *vrow = m.dist + (uint64_t)v * R;
     uint32_t qm = 0;
 #pragma unroll
-    for (int q = 0; q < 16; q++) qm |= ((f >> (4 * q)) & 0xfull) ? 1u << q : 0u;
+    for (int q = 0; q < R / 4; q++) qm |= ((f >> (4 * q)) & 0xfull) ? 1u << q : 0u;
     unsigned long long imp = 0;
     while (qm) {
         int qx[kMsQuads];
@@ -2236,9 +2241,10 @@ __device__ __forceinline__ void ms_sssp_lane_quads(const MsArgs &m, uint32_t u, 
 // [e0, e0 + 32) ∩ [0, total). An edge whose source vertex is active for at most
 // kMsQuadSources sources is relaxed by its own lane for each of them; the
 // others are gathered into the warp's shared slots and relaxed by groups of
-// kMsLanes lanes, each lane kMsPerLane sources (16-byte loads of the source's
-// and the destination's 256-byte distance rows), kMsRows edges per group in
-// flight.
+// R / kMsPerLane lanes, each lane kMsPerLane sources (16-byte loads of the
+// source's and the destination's distance rows of R x 4 bytes), kMsRows edges
+// per group in flight.
+template <int R>
 __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs &a, MsSsspSmem &sm, uint32_t e0,
                                               uint32_t total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -2263,7 +2269,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
         // few sources: this lane relaxes its edge for each of them, loading the
         // values of kMsGroup sources before comparing any
         const uint32_t u = sm.vid[o];
-        uint32_t *row = m.dist + (uint64_t)v * kMaxBatch;
+        uint32_t *row = m.dist + (uint64_t)v * R;
         unsigned long long fm = f, imp = 0;
         while (fm) {
             uint32_t ds[kMsGroup], cur[kMsGroup];
@@ -2272,7 +2278,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
             for (int k = 0; k < kMsGroup; k++) {
                 sx[k] = fm ? __ffsll((long long)fm) - 1 : -1;
                 fm &= fm - 1;
-                ds[k] = sx[k] >= 0 ? m.dist[(uint64_t)u * kMaxBatch + sx[k]] : 0u;
+                ds[k] = sx[k] >= 0 ? m.dist[(uint64_t)u * R + sx[k]] : 0u;
                 cur[k] = sx[k] >= 0 ? row[sx[k]] : 0u;
             }
 #pragma unroll
@@ -2293,7 +2299,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
             atomicOr(&m.touched[v >> 5], 1u << (v & 31));
         }
     }
-    if (ok && mid) ms_sssp_lane_quads(m, sm.vid[o], v, w, f);
+    if (ok && mid) ms_sssp_lane_quads<R>(m, sm.vid[o], v, w, f);
     const uint32_t dm = __ballot_sync(kFull, ok && dense);
     if (!dm) return;
     if (ok && dense) {
@@ -2304,8 +2310,8 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
     }
     __syncwarp();
     const uint32_t nd = __popc(dm);
-    // kMsLanes lanes per edge, kMsPerLane sources (kMsPerLane / 4 quads) per lane
-    constexpr int G = kMsLanes, S = kMsPerLane, Q = kMsPerLane / 4, EPW = 32 / kMsLanes;
+    // R / kMsPerLane lanes per edge, kMsPerLane sources (kMsPerLane / 4 quads) per lane
+    constexpr int S = kMsPerLane < R ? kMsPerLane : R, G = R / S, Q = S / 4, EPW = 32 / G;
     const uint32_t grp = (uint32_t)lane / G, l = (uint32_t)lane % G;
     for (uint32_t j0 = 0; j0 < nd; j0 += EPW * kMsRows) {
         uint32_t vk[kMsRows], wk[kMsRows], act[kMsRows];
@@ -2327,8 +2333,8 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
                 wk[k] = sm.dw[wid][j];
                 act[k] = (uint32_t)(sm.f[ow] >> (S * l)) & (uint32_t)((1ull << S) - 1);
                 if (act[k]) {
-                    const uint4 *ur = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)sm.vid[ow] * kMaxBatch);
-                    const uint4 *vr = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)vk[k] * kMaxBatch);
+                    const uint4 *ur = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)sm.vid[ow] * R);
+                    const uint4 *vr = reinterpret_cast<const uint4 *>(m.dist + (uint64_t)vk[k] * R);
 #pragma unroll
                     for (int q = 0; q < Q; q++) {
                         du[k][q] = ur[Q * l + q];
@@ -2342,7 +2348,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
             const uint32_t j = j0 + EPW * k + grp;
             uint32_t imp = 0;
             if (act[k]) {
-                uint32_t *row = m.dist + (uint64_t)vk[k] * kMaxBatch + S * l;
+                uint32_t *row = m.dist + (uint64_t)vk[k] * R + S * l;
 #pragma unroll
                 for (int q = 0; q < Q; q++) {
                     const uint32_t n0 = du[k][q].x + wk[k], n1 = du[k][q].y + wk[k];
@@ -2372,6 +2378,7 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
 // segment of a long list. The tile's edges are walked as one flattened range,
 // 32 per warp per pass, so short lists do not leave lanes idle and every warp
 // has loads in flight.
+template <int R>
 __device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, uint32_t n_in, uint32_t nseg,
                              MsSsspSmem &sm) {
     bool act = false;
@@ -2409,7 +2416,7 @@ __device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, u
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(act);
     for (uint32_t base = 0; base < total; base += kBlock)
-        ms_sssp_chunk(m, a, sm, base + (threadIdx.x & ~31u), total);
+        ms_sssp_chunk<R>(m, a, sm, base + (threadIdx.x & ~31u), total);
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
         atomicAdd(&a.stats[2 + a.region], (unsigned long long)nact);
@@ -2420,7 +2427,9 @@ __device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, u
 // Work items are per CTA: the static region's segments and list tiles and the
 // on-demand region's, interleaved so link-bound and HBM-bound work overlap.
 // The SSSP batch always builds lists (its RegionArgs carry dense_div = 0).
+template <int R>
 __global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_sssp_expand_kernel(MsArgs m) {
+    static_assert(ms_row_ok(R), "rows of 16, 32 or 64 sources");
     __shared__ MsSsspSmem sm;
     uint32_t n0, s0, i0, n1, s1, i1;
     bool m0, m1;
@@ -2442,8 +2451,8 @@ __global__ void __launch_bounds__(kBlock, ASC_MS_MIN_BLOCKS) ms_sssp_expand_kern
             od = i1 > i0;
             local = mm + (w - 2 * mm);
         }
-        if (od) ms_sssp_item(m, m.r1, local, n1, s1, sm);
-        else ms_sssp_item(m, m.r0, local, n0, s0, sm);
+        if (od) ms_sssp_item<R>(m, m.r1, local, n1, s1, sm);
+        else ms_sssp_item<R>(m, m.r0, local, n0, s0, sm);
     }
 }
 
@@ -2528,13 +2537,14 @@ struct Admit {
 __global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint32_t stride, uint32_t **planes,
                                 unsigned long long newmask, uint32_t V, uint32_t fill, uint32_t sssp) {
     if (sssp) {
-        // a half-warp per distance row (stride 64): lane l owns sources
-        // 4l..4l+3, one 16-byte store when all four are new, else a merge
-        const uint32_t l = threadIdx.x & 15u;
+        // stride / 4 lanes per distance row (16 for 64 sources): lane l owns
+        // sources 4l..4l+3, one 16-byte store when all four are new, else a merge
+        const uint32_t lanes = stride / 4;
+        const uint32_t l = threadIdx.x % lanes;
         const uint32_t m4 = (uint32_t)(newmask >> (4 * l)) & 0xfu;
         if (!m4) return;
-        const uint64_t h0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-        const uint64_t hs = ((uint64_t)gridDim.x * blockDim.x) >> 4;
+        const uint64_t h0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / lanes;
+        const uint64_t hs = ((uint64_t)gridDim.x * blockDim.x) / lanes;
         for (uint64_t v = h0; v < V; v += hs) {
             uint4 *p = reinterpret_cast<uint4 *>(dist + v * stride) + l;
             uint4 x = make_uint4(fill, fill, fill, fill);
@@ -2645,7 +2655,9 @@ asc_status batch_create(asc_graph *g, bool sssp, uint32_t stride, BatchEngine **
     b->g = g;
     b->sssp = sssp;
     b->stride = stride;
-    asc_status st = stride == 64 ? ASC_OK : fail(ASC_ERR_UNSUPPORTED, "batch rows of %u sources", stride);
+    asc_status st = stride == 64 || (sssp && (stride == 16 || stride == 32))
+                        ? ASC_OK
+                        : fail(ASC_ERR_UNSUPPORTED, "batch rows of %u sources", stride);
     // 64-source batches keep the default thresholds: a graph's tuning is chosen on
     // single-source runs, and the batch kernels measured faster with the defaults
     if (st == ASC_OK) st = alloc_workspace(g, &b->ws, false);
@@ -2709,6 +2721,8 @@ asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source) {
 
 bool batch_busy(const BatchEngine *b) { return b->active != 0; }
 
+uint32_t batch_slots(const BatchEngine *b) { return b->sssp ? b->stride : 64u; }
+
 // Applies the queued admissions and launches one iteration on the batch's
 // stream, ending with the readback of its counts (nothing waits here).
 asc_status batch_launch(BatchEngine *b) {
@@ -2755,7 +2769,9 @@ asc_status batch_launch(BatchEngine *b) {
     m.work = m.r0.cnt_out + 4;
     const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
     b->it++;
-    if (b->sssp) ms_sssp_expand_kernel<<<grid, kBlock, 0, s>>>(m);
+    if (b->sssp && b->stride == 16) ms_sssp_expand_kernel<16><<<grid, kBlock, 0, s>>>(m);
+    else if (b->sssp && b->stride == 32) ms_sssp_expand_kernel<32><<<grid, kBlock, 0, s>>>(m);
+    else if (b->sssp) ms_sssp_expand_kernel<64><<<grid, kBlock, 0, s>>>(m);
     else if (g->edge_words == 2) ms_bfs_expand_kernel<2><<<grid, kBlock, 0, s>>>(m);
     else if (g->ebits < 32) ms_bfs_expand_kernel<kBitsLayout><<<grid, kBlock, 0, s>>>(m);
     else ms_bfs_expand_kernel<1><<<grid, kBlock, 0, s>>>(m);

@@ -173,10 +173,22 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
             }
             if (!pend.empty() && !gs.batch[k]) {
                 const bool sssp = k == 1;
-                uint64_t need = asc::batch_state_bytes(gs.g, sssp, 64);
+                // SSSP keeps a row of distances per vertex, one column per
+                // slot: rows of 64 sources, or of 32 or 16 where max_batch asks
+                // for no more or where 64 columns of this graph could never fit
+                // the budget
+                uint32_t stride = 64;
+                if (sssp) {
+                    while (stride > 16 && stride / 2 >= max_batch) stride /= 2;
+                    while (stride > 16 && s->cfg.device_budget_bytes &&
+                           asc::batch_state_bytes(gs.g, true, stride) + s->used_bytes - batch_held(s) >
+                               s->cfg.device_budget_bytes)
+                        stride /= 2;
+                }
+                uint64_t need = asc::batch_state_bytes(gs.g, sssp, stride);
                 if (need <= budget_left(s)) {
                     asc::BatchEngine *b = nullptr;
-                    asc_status st = asc::batch_create(gs.g, sssp, 64, &b);
+                    asc_status st = asc::batch_create(gs.g, sssp, stride, &b);
                     if (st == ASC_OK) {
                         gs.batch[k] = b;
                         gs.batch_bytes[k] = need;
@@ -199,7 +211,8 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
             }
             asc::BatchEngine *b = gs.batch[k];
             if (!b) continue;
-            for (uint32_t slot = 0; slot < max_batch && !pend.empty(); slot++) {
+            const uint32_t slots = std::min(max_batch, asc::batch_slots(b));
+            for (uint32_t slot = 0; slot < slots && !pend.empty(); slot++) {
                 if (gs.slot_q[k][slot]) continue;
                 if (k == 0 && !asc::batch_has_plane(b, slot)) {
                     if (asc::batch_plane_bytes(gs.g) > budget_left(s)) break;

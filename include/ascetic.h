@@ -266,7 +266,8 @@ enum { ASC_SERVE_BATCHED = 0, ASC_SERVE_FIFO = 1 };
 
 typedef struct asc_server_config {
     uint64_t device_budget_bytes; /* every device allocation of the graphs and queries (0 = no cap) */
-    uint32_t max_batch;           /* sources per batch, 1..64 (0 = 64) */
+    uint32_t max_batch;           /* sources per batch, 1..64 (0 = 64); SSSP batches of at most 16 or
+                                     32 sources keep rows of that width (less device memory) */
     uint32_t queue_capacity;      /* queries in flight before ASC_ERR_BUSY (0 = 2^20) */
     uint32_t mode;                /* ASC_SERVE_BATCHED or ASC_SERVE_FIFO */
     uint32_t reserved;

@@ -147,3 +147,24 @@ def test_tight_shared_budget_completes(extra):
             assert np.array_equal(out, oracle.cc(ptr, adj[:, 0]))
     for g in graphs:
         g.close()
+
+
+@pytest.mark.parametrize("max_batch", [12, 32])
+def test_narrow_sssp_batches_equal_solo_runs(max_batch):
+    """A server whose max_batch is at most 32 (or whose budget cannot hold 64
+    distance columns of a graph) runs SSSP batches with rows of 16 or 32
+    sources; every query still gets the solo values."""
+    ptr, adj = A.rmat_csr(13, 16, 61, weights=(1, 63))
+    deg = np.diff(ptr)
+    rng = np.random.default_rng(max_batch)
+    srcs = rng.choice(np.nonzero(deg)[0], size=70, replace=False).tolist()
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=0.25)) as g:
+        with A.Server(max_batch=max_batch) as srv:
+            gid = srv.add_graph(g)
+            tickets = [srv.submit(gid, "sssp", s) for s in srcs]
+            results = [srv.wait(t, timeout_ms=120000) for t in tickets]
+            st = srv.stats()
+    assert st["completed"] == len(srcs) and st["failed"] == 0
+    for s, (out, info) in zip(srcs, results):
+        assert info["status"] == A.OK and 1 <= info["batch_size"] <= max_batch
+        assert np.array_equal(out, oracle.sssp(ptr, adj, s)), s
