@@ -1991,6 +1991,14 @@ __device__ __forceinline__ void mark_touched(const MsArgs &m, bool first, uint32
     if (first) atomicOr(&m.touched[v >> 5], 1u << (v & 31));
 }
 
+#ifndef ASC_MS_UNROLL
+#define ASC_MS_UNROLL 4
+#endif
+// Edges per thread per pass in the batched BFS expansion (all loads first).
+// 64-source batch, RMAT scale 22 / 24: 5.45 / 18.27 ms at 4 (32 registers, 8
+// CTAs per SM), 5.58 / 18.46 at 6 (40, 6 CTAs), 5.78 / 18.96 at 8 (48, 5 CTAs).
+constexpr int kMsUnroll = ASC_MS_UNROLL;
+
 template <int WORDS>
 __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint32_t u, MsSmem &sm) {
     uint32_t deg = 0, start = 0;
@@ -2011,11 +2019,11 @@ __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint
     sm.f[threadIdx.x] = f;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(act);
-    for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
-        uint32_t v[kUnroll];
-        unsigned long long fk[kUnroll], vis[kUnroll];
+    for (uint32_t base = 0; base < total; base += kMsUnroll * kBlock) {
+        uint32_t v[kMsUnroll];
+        unsigned long long fk[kMsUnroll], vis[kMsUnroll];
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) {
+        for (int k = 0; k < kMsUnroll; k++) {
             const uint32_t e = base + k * kBlock + threadIdx.x;
             v[k] = 0;
             fk[k] = 0;
@@ -2032,9 +2040,9 @@ __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint
             }
         }
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) vis[k] = fk[k] ? m.visit[v[k]] : ~0ull;
+        for (int k = 0; k < kMsUnroll; k++) vis[k] = fk[k] ? m.visit[v[k]] : ~0ull;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) mark_touched(m, ms_reach(m, v[k], fk[k], vis[k]), v[k]);
+        for (int k = 0; k < kMsUnroll; k++) mark_touched(m, ms_reach(m, v[k], fk[k], vis[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)total);
@@ -2051,21 +2059,21 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     const unsigned long long f = m.front[u];
-    for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
-        uint32_t v[kUnroll];
-        unsigned long long vis[kUnroll];
-        bool ok[kUnroll];
+    for (uint32_t base = 0; base < n; base += kMsUnroll * kBlock) {
+        uint32_t v[kMsUnroll];
+        unsigned long long vis[kMsUnroll];
+        bool ok[kMsUnroll];
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) {
+        for (int k = 0; k < kMsUnroll; k++) {
             const uint32_t j = base + k * kBlock + threadIdx.x;
             ok[k] = j < n;
             v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : layout_word<WORDS>(a.edges, b + j, a.ebits) >> a.wbits)
                          : 0;
         }
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
+        for (int k = 0; k < kMsUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
 #pragma unroll
-        for (int k = 0; k < kUnroll; k++) mark_touched(m, ok[k] && ms_reach(m, v[k], f, vis[k]), v[k]);
+        for (int k = 0; k < kMsUnroll; k++) mark_touched(m, ok[k] && ms_reach(m, v[k], f, vis[k]), v[k]);
     }
     if (threadIdx.x == 0) {
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
