@@ -2126,8 +2126,8 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 }
 
 // Batched SSSP expansion: one CTA per work item (a tile of frontier vertices,
-// or one segment of a long list); the 64 distances of a vertex are one
-// 256-byte row of dist.
+// or one segment of a long list); the distances of a vertex are one row of
+// dist (64 sources: 256 bytes).
 #ifndef ASC_MS_SSSP_SPARSE
 #define ASC_MS_SSSP_SPARSE 4
 #endif
@@ -2135,10 +2135,10 @@ __global__ void __launch_bounds__(kBlock) ms_bfs_expand_kernel(MsArgs m) {
 // relaxed lane-per-edge, one 4-byte load per source and row; up to
 // kMsQuadSources lane-per-edge a 16-byte quad of sources at a time; above that
 // a group of lanes per edge. 64- and 8-source batches on RMAT scale 24 (16 lanes
-// per many-source edge): 4-byte
-// loads up to 8 sources and half-warps above: 75 / 30 ms; quads for 5-8: 75 /
-// 26 ms; quads up to 12 or 16: 79-81 / 26 ms; quads for all above 4: 150 / 26
-// ms; 4-byte loads up to 16, 32 or 64 sources: 82, 101, 179 ms (64 sources).
+// per many-source edge): 4-byte loads up to 8 sources and half-warps above: 75 /
+// 30 ms; quads for 5-8: 75 / 26 ms; quads up to 12 or 16: 79-81 / 26 ms; quads
+// for all above 4: 150 / 26 ms; 4-byte loads up to 16, 32 or 64 sources: 82,
+// 101, 179 ms (64 sources).
 constexpr int kMsSparseSources = ASC_MS_SSSP_SPARSE;
 // Sources whose values a lane of the few-source path loads before comparing.
 constexpr int kMsGroup = kMsSparseSources < 8 ? kMsSparseSources : 8;
