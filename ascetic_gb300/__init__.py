@@ -408,7 +408,12 @@ Graph.set_tuning = _set_tuning
 
 
 class Server:
-    """Query server over resident graphs (continuous batching or FIFO)."""
+    """Query server over resident graphs (continuous batching or FIFO).
+
+    budget_bytes caps every device allocation the server makes (0: no cap);
+    max_batch (1..64) caps the sources of one batch, and an SSSP batch of at
+    most 16 or 32 sources keeps distance rows of that width, as it does when
+    64 columns of a graph could never fit the budget."""
 
     def __init__(self, budget_bytes=0, mode=SERVE_BATCHED, max_batch=64):
         cfg = ServerConfig()
