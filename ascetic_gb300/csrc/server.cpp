@@ -74,6 +74,7 @@ struct asc_server {
     bool stop = false;
     bool started = false;
     int single_graph = -1;          // graph the single worker is running, -1 when idle
+    int device = -1;                // the device every graph of this server was opened on
     std::thread batch_worker, single_worker;
     std::vector<double> lat_ms;
     uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, batches = 0, batch_sources = 0;
@@ -236,7 +237,8 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
 }
 
 void batch_loop(asc_server *s) {
-    cudaSetDevice(0);
+    // the graphs' device (asc_server_add_graph admits graphs of one device only)
+    if (s->device >= 0) cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
         std::vector<std::pair<uint32_t, int>> work;
@@ -313,7 +315,7 @@ void batch_loop(asc_server *s) {
 }
 
 void single_loop(asc_server *s) {
-    cudaSetDevice(0);
+    if (s->device >= 0) cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
         while (!s->single.empty() && s->single.front()->cancel) {
@@ -440,6 +442,10 @@ asc_status asc_server_add_graph(asc_server *s, asc_graph *g, uint32_t *graph_id)
     if (!s || !g || !graph_id) return fail(ASC_ERR_INVALID, "asc_server_add_graph: null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->started) return fail(ASC_ERR_INVALID, "add graphs before the first query");
+    // the workers run every graph's kernels with one device current
+    if (s->device >= 0 && g->device != s->device)
+        return fail(ASC_ERR_INVALID, "graph was opened on device %d, this server's graphs on device %d", g->device,
+                    s->device);
     asc_graph_info info;
     asc_graph_info_get(g, &info);
     GraphSlot gs;
@@ -453,6 +459,7 @@ asc_status asc_server_add_graph(asc_server *s, asc_graph *g, uint32_t *graph_id)
         return fail(ASC_ERR_BUDGET, "graph needs %llu device bytes, %llu of the budget left",
                     (unsigned long long)(gs.base_bytes + gs.ws_bytes), (unsigned long long)budget_left(s));
     s->used_bytes += gs.base_bytes + gs.ws_bytes;
+    s->device = g->device;
     *graph_id = (uint32_t)s->graphs.size();
     s->graphs.push_back(gs);
     return ASC_OK;

@@ -15,7 +15,7 @@ manifest.json lists the runs. For every run two results are stored:
                   stays zero (hazard_mode 0, GraphMeta.cuh:230-233).
 
 Usage (needs the reference tree, so it runs only where the fixtures are made):
-    make -C oracle/refemu && python tests/golden/make_golden.py
+    make -C oracle/refemu REF=<reference tree> && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -118,7 +118,7 @@ def edge_case_graphs():
 
 def main():
     if not os.path.exists(REF_LIB):
-        sys.exit("build the reference emulation first: make -C oracle/refemu")
+        sys.exit("build the reference emulation first: make -C oracle/refemu REF=<reference tree>")
     lib = load_ref()
     tmp = tempfile.mkdtemp()
     manifest = {"graphs": {}}

@@ -3,15 +3,17 @@
 It is for callers that cannot allocate device memory at query time (their
 device memory belongs to another allocator, or cudaMalloc/cudaFree are not
 allowed in their loop); its scratch is a fixed device array inside the library.
-The test checks it against the regular entry point (asc_run) on the same graph,
-bit for bit, on two calls in a row, plus its limit and input checks. The graph
-is placed in device memory with torch, which stands in for the caller's own
-allocator. This file is collected last.
+The test checks it against the regular entry point (asc_run) and against the
+CPU oracle on the same graph, bit for bit, on two calls in a row (the first on
+the default stream, the second on a stream of the caller's), plus its limit and
+input checks. The graph is placed in device memory with torch, which stands in
+for the caller's own allocator. This file is collected last.
 """
 import numpy as np
 import pytest
 
 import ascetic_gb300 as A
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -30,12 +32,17 @@ def test_noalloc_bfs_matches_asc_run_on_two_calls():
     d_ptr = _device(torch, ptr.astype(np.uint32))
     d_col = _device(torch, col)
     d_out = torch.empty(V, dtype=torch.int32, device="cuda")
-    for s, exp in zip(sources, expected):
-        rc = A.lib().asc_bfs_device_noalloc(V, E, d_ptr.data_ptr(), d_col.data_ptr(), s, d_out.data_ptr(), None)
+    torch.cuda.synchronize()
+    # the second call runs on a stream of the caller's (its cudaStream_t handle)
+    streams = [None, torch.cuda.Stream()]
+    for s, exp, stream in zip(sources, expected, streams):
+        handle = None if stream is None else stream.cuda_stream
+        rc = A.lib().asc_bfs_device_noalloc(V, E, d_ptr.data_ptr(), d_col.data_ptr(), s, d_out.data_ptr(), handle)
         torch.cuda.synchronize()
         assert rc == A.OK, A.last_error()
         got = d_out.cpu().numpy().view(np.uint32)
         assert np.array_equal(got, exp), s
+        assert np.array_equal(got, oracle.bfs(ptr, col, s)), s
 
 
 def test_noalloc_rejects_sizes_and_bad_csr():
