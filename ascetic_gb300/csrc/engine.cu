@@ -740,45 +740,85 @@ __global__ void reached_kernel(const uint32_t *val, const uint32_t *ptr, uint32_
 }
 
 // ------------------------------------------------------------- PageRank -----
+//
+// Ranks are FP64 in every mode; the contributions rank/outDeg that the edges
+// carry are T (FP64, or FP32 for the precision pattern: 4 bytes per edge
+// gather, and half the L2 footprint of the contribution array).
+//
+// How the sums of contributions accumulate (PrAcc<T>): FP64 contributions add
+// in FP64, where the order of the atomics changes a sum by about 1e-16
+// relative, far below the stop tolerance. FP32 contributions add exactly, as
+// 64-bit fixed point with 62 fraction bits. Integer addition is associative,
+// so a vertex's sum does not depend on how its edges are split over lanes,
+// warps, tiles, segments or atomics: every pass recomputes bit-identical sums
+// from identical contributions, and the FP64 L1 residual falls to the stop
+// tolerance. (FP32 atomics in any order floor it near 1.5e-8 at RMAT scale
+// 25, so that such a run always took the pass cap.) A sum is at most the total
+// rank (1 in standard mode), so two integer bits are enough; a contribution
+// below 2^-62 rounds to the grid (an absolute error below 1.1e-19 per edge).
+template <typename T>
+struct PrAcc;
+template <>
+struct PrAcc<double> {
+    typedef double type;
+    static __device__ __forceinline__ double from(double x) { return x; }
+    static __device__ __forceinline__ double value(double a) { return a; }
+};
+template <>
+struct PrAcc<float> {
+    typedef unsigned long long type;
+    static __device__ __forceinline__ unsigned long long from(float x) { return __float2ull_rn(x * 0x1p62f); }
+    static __device__ __forceinline__ double value(unsigned long long a) { return __ull2double_rn(a) * 0x1p-62; }
+};
 
 template <typename T>
 struct PrArgs {
+    typedef typename PrAcc<T>::type Acc;
     RegionArgs r;           // lists, segments, counts (pull over in-edges)
     const uint32_t *outdeg;
-    T *rank;
+    double *rank;
     const T *c_old;
     T *c_new;
-    T *sum;                 // partial sums of segmented vertices
+    Acc *sum;               // partial sums of segmented vertices
     double damping;
     const double *dangling_prev;   // std mode: dangling mass of the previous pass
     double *acc;            // std mode: [0] residual, [1] dangling of this pass
 };
 
-template <typename T, bool REF>
-__device__ __forceinline__ bool pr_apply(const PrArgs<T> &p, uint32_t v, T s, double &res, double &dang) {
-    const uint32_t od = p.outdeg[v];
-    if (REF) {
-        const double r = (double)p.rank[v];
-        const double t = fma(0.85, (double)s, 0.15);
+// The update of one vertex from its summed contributions s (FP64):
+// reference mode prKernel_Opt (gpu_kernels.cuh:533-552), standard mode
+// (1 - d) / V + d * (dangling mass / V + s) with the L1 residual and the
+// dangling mass of this pass accumulated in FP64.
+template <typename T>
+__device__ __forceinline__ bool pr_update(double *rank, const T *c_old, T *c_new, uint32_t v, uint32_t od, double s,
+                                          bool ref, double damping, double V, const double *dangling_prev,
+                                          double &res, double &dang) {
+    if (ref) {
+        const double r = rank[v];
+        const double t = fma(0.85, s, 0.15);
         const double diff = t > r ? t - r : r - t;
         if (diff > 0.001) {
-            p.rank[v] = (T)t;
-            p.c_new[v] = od ? (T)(t / (double)od) : (T)0;
+            rank[v] = t;
+            c_new[v] = od ? (T)(t / (double)od) : (T)0;
             return true;
         }
-        p.c_new[v] = p.c_old[v];
-        return false;
-    } else {
-        const double Vd = (double)p.r.V;
-        const T base = (T)((1.0 - p.damping) / Vd + p.damping * (*p.dangling_prev) / Vd);
-        const T r = p.rank[v];
-        const T rn = base + (T)p.damping * s;
-        res += fabs((double)rn - (double)r);
-        if (od == 0) dang += (double)rn;
-        p.rank[v] = rn;
-        p.c_new[v] = od ? rn / (T)od : (T)0;
+        c_new[v] = c_old[v];
         return false;
     }
+    const double base = (1.0 - damping) / V + damping * (*dangling_prev) / V;
+    const double r = rank[v];
+    const double rn = base + damping * s;
+    res += fabs(rn - r);
+    if (od == 0) dang += rn;
+    rank[v] = rn;
+    c_new[v] = od ? (T)(rn / (double)od) : (T)0;
+    return false;
+}
+
+template <typename T, bool REF>
+__device__ __forceinline__ bool pr_apply(const PrArgs<T> &p, uint32_t v, double s, double &res, double &dang) {
+    return pr_update<T>(p.rank, p.c_old, p.c_new, v, p.outdeg[v], s, REF, p.damping, (double)p.r.V,
+                        p.dangling_prev, res, dang);
 }
 
 template <typename T>
@@ -811,7 +851,7 @@ struct PrSmem {
     uint32_t pref[kBlock + 1];
     uint32_t start[kBlock];
     uint32_t warp[kWarps + 1];
-    T sum[kBlock];
+    typename PrAcc<T>::type sum[kBlock];
     double red[2 * kWarps];
     uint32_t work;
 };
@@ -821,6 +861,7 @@ struct PrSmem {
 // bit in the next bitmap; standard mode walks every vertex of the region.
 template <typename T, bool REF>
 __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T> &sm, uint32_t *s_next) {
+    typedef typename PrAcc<T>::type Acc;
     const RegionArgs &a = p.r;
     uint32_t deg = 0, start = 0;
     bool huge = false;
@@ -834,13 +875,13 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
     uint32_t excl = block_excl_scan(deg, total, sm.warp);
     sm.pref[threadIdx.x] = excl;
     sm.start[threadIdx.x] = start;
-    sm.sum[threadIdx.x] = (T)0;
+    sm.sum[threadIdx.x] = (Acc)0;
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(valid && !huge);
     const int lane = threadIdx.x & 31;
     for (uint32_t base = 0; base < total; base += kBlock) {
         const uint32_t e = base + threadIdx.x;
-        T x = (T)0;
+        Acc x = (Acc)0;
         int owner = -1 - lane;  // distinct per invalid lane
         if (e < total) {
             int lo = 0, hi = kBlock;
@@ -851,12 +892,12 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
             }
             owner = lo;
             const uint32_t srcv = edge_word(a.edges, (uint64_t)sm.start[lo] + (e - sm.pref[lo]), a.ebits);
-            x = p.c_old[srcv];
+            x = PrAcc<T>::from(p.c_old[srcv]);
         }
         // segmented suffix sum over lanes with the same owner (owners ascend with the lane)
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            T y = __shfl_down_sync(kFull, x, d);
+            Acc y = __shfl_down_sync(kFull, x, d);
             int oy = __shfl_down_sync(kFull, owner, d);
             if (lane + d < 32 && oy == owner) x += y;
         }
@@ -866,7 +907,7 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
     __syncthreads();
     double res = 0, dang = 0;
     bool won = false;
-    if (valid && !huge) won = pr_apply<T, REF>(p, u, sm.sum[threadIdx.x], res, dang);
+    if (valid && !huge) won = pr_apply<T, REF>(p, u, PrAcc<T>::value(sm.sum[threadIdx.x]), res, dang);
     if (REF) {
         if (won) atomicOr(&a.bitmap[u >> 5], 1u << (u & 31));
         count_next(a, won, u, s_next);
@@ -906,21 +947,22 @@ __device__ void pr_bitmap_tile(const PrArgs<T> &p, uint32_t tile, PrSmem<T> &sm,
 
 template <typename T>
 __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
+    typedef typename PrAcc<T>::type Acc;
     const RegionArgs &a = p.r;
     const uint32_t u = (uint32_t)(item >> 32), k = (uint32_t)item;
     const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
     const uint64_t b = (uint64_t)b0 + (uint64_t)k * a.seg_len;
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
-    T x = (T)0;
-    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += p.c_old[edge_word(a.edges, b + j, a.ebits)];
+    Acc x = (Acc)0;
+    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += PrAcc<T>::from(p.c_old[edge_word(a.edges, b + j, a.ebits)]);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(kFull, x, d);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) sm.sum[w] = x;
     __syncthreads();
     if (threadIdx.x == 0) {
-        T s = (T)0;
+        Acc s = (Acc)0;
         for (int i = 0; i < kWarps; i++) s += sm.sum[i];
         atomicAdd(&p.sum[u], s);
         atomicAdd(&a.stats[a.region], (unsigned long long)n);
@@ -1044,8 +1086,8 @@ __global__ void pr_apply_segmented_kernel(PrArgs<T> p, const uint64_t *items_sta
                 v = huge_list[i];
             }
             if (go) {
-                T s = p.sum[v];
-                p.sum[v] = (T)0;
+                const double s = PrAcc<T>::value(p.sum[v]);
+                p.sum[v] = 0;
                 won = pr_apply<T, REF>(p, v, s, res, dang);
             }
         }
@@ -1063,7 +1105,8 @@ __global__ void pr_apply_segmented_kernel(PrArgs<T> p, const uint64_t *items_sta
 }
 
 template <typename T>
-__global__ void pr_init_kernel(T *rank, T *c0, T *c1, T *sum, const uint32_t *outdeg, uint32_t V, double *dang) {
+__global__ void pr_init_kernel(double *rank, T *c0, T *c1, typename PrAcc<T>::type *sum, const uint32_t *outdeg,
+                               uint32_t V, double *dang) {
     // dang points at a (residual, dangling) pair; the start vector adds to dangling
     __shared__ double red[2 * kWarps];
     double d = 0;
@@ -1073,15 +1116,22 @@ __global__ void pr_init_kernel(T *rank, T *c0, T *c1, T *sum, const uint32_t *ou
         if (i < V) {
             const double r = 1.0 / (double)V;
             const uint32_t od = outdeg[i];
-            rank[i] = (T)r;
+            rank[i] = r;
             const T c = od ? (T)(r / (double)od) : (T)0;
             c0[i] = c;
             c1[i] = c;
-            sum[i] = (T)0;
-            if (od == 0) d += (double)(T)r;
+            sum[i] = 0;
+            if (od == 0) d += r;
         }
     }
     block_reduce2_atomic<T>(0.0, d, dang, red);
+}
+
+// FP32 results: the FP64 ranks rounded to float (into the caller's device
+// buffer, or a staging buffer that is then copied out).
+__global__ void pr_rank_to_float_kernel(const double *rank, float *out, uint32_t V) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
+        out[i] = (float)rank[i];
 }
 
 // Segment items of every long-list vertex (standard PageRank, fixed each pass).
@@ -1164,19 +1214,24 @@ asc_status ensure_workspace(asc_graph *g) {
     return alloc_workspace(g, g->ws);
 }
 
+// PageRank state for contributions of elem bytes: FP64 ranks, two
+// contribution arrays (this pass's and the next's), 8-byte sums.
+uint64_t pr_buffer_bytes(uint64_t V, size_t elem) { return (16 + 2 * (uint64_t)elem) * V; }
+
 asc_status ensure_pr_buffers(asc_graph *g, size_t elem) {
     Workspace *ws = g->ws;
     if (ws->pr_rank && ws->pr_elem == elem) return ASC_OK;
     for (void *p : {ws->pr_rank, ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
         if (p) cudaFree(p);
-    if (ws->pr_rank) ws->device_bytes -= 4 * ws->pr_elem * g->V;
+    if (ws->pr_rank && ws->pr_elem) ws->device_bytes -= pr_buffer_bytes(g->V, ws->pr_elem);
     ws->pr_rank = ws->pr_contrib[0] = ws->pr_contrib[1] = ws->pr_sum = nullptr;
-    ASC_CUDA(cudaMalloc(&ws->pr_rank, elem * g->V));
+    ws->pr_elem = 0;
+    ASC_CUDA(cudaMalloc(&ws->pr_rank, 8 * g->V));
     ASC_CUDA(cudaMalloc(&ws->pr_contrib[0], elem * g->V));
     ASC_CUDA(cudaMalloc(&ws->pr_contrib[1], elem * g->V));
-    ASC_CUDA(cudaMalloc(&ws->pr_sum, elem * g->V));
+    ASC_CUDA(cudaMalloc(&ws->pr_sum, 8 * g->V));
     ws->pr_elem = elem;
-    ws->device_bytes += 4 * elem * g->V;
+    ws->device_bytes += pr_buffer_bytes(g->V, elem);
     return ASC_OK;
 }
 
@@ -1763,6 +1818,25 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     return ASC_OK;
 }
 
+// Copies the FP64 ranks out as T: directly for FP64; for FP32 rounded to
+// float on the device, into the caller's buffer (ASC_RUN_DEVICE_OUT) or into
+// staging (a contribution array, free once the passes are over) copied out.
+template <typename T>
+asc_status copy_ranks_out(asc_graph *g, const double *rank, void *staging, void *out, uint32_t flags) {
+    const uint32_t V = (uint32_t)g->V;
+    cudaStream_t s = g->stream;
+    const cudaMemcpyKind kind = (flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (sizeof(T) == 8) {
+        ASC_CUDA(cudaMemcpyAsync(out, rank, 8 * (size_t)V, kind, s));
+        return ASC_OK;
+    }
+    float *dst = (flags & ASC_RUN_DEVICE_OUT) ? (float *)out : (float *)staging;
+    pr_rank_to_float_kernel<<<fill_grid(g->ws, V), kBlock, 0, s>>>(rank, dst, V);
+    ASC_CUDA(cudaGetLastError());
+    if (!(flags & ASC_RUN_DEVICE_OUT)) ASC_CUDA(cudaMemcpyAsync(out, staging, 4 * (size_t)V, kind, s));
+    return ASC_OK;
+}
+
 template <typename T, bool REF>
 static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, asc_stats *st) {
     Workspace *ws = g->ws;
@@ -1771,15 +1845,16 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
     cudaStream_t s = g->stream;
     uint32_t launches = 0;
     PhaseTimer pt(ws, (p.flags & ASC_RUN_PHASE_TIMING) != 0);
+    typedef typename PrAcc<T>::type Acc;
     // FP64 accumulators per pass parity q: acc[2q] residual, acc[2q+1] dangling mass
     double *acc = (double *)(ws->ctl + CTL_PR);
-    T *rank = (T *)ws->pr_rank;
+    double *rank = (double *)ws->pr_rank;
     T *c[2] = {(T *)ws->pr_contrib[0], (T *)ws->pr_contrib[1]};
 
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
     // the start vector's dangling mass goes to the parity-1 pair, which pass 0 reads
-    pr_init_kernel<T><<<fill_grid(ws, V), kBlock, 0, s>>>(rank, c[0], c[1], (T *)ws->pr_sum, g->d_outdeg, V,
+    pr_init_kernel<T><<<fill_grid(ws, V), kBlock, 0, s>>>(rank, c[0], c[1], (Acc *)ws->pr_sum, g->d_outdeg, V,
                                                           acc + 2);
     launches++;
     RegionArgs sa = base_args(g, 1);  // seeds land in parity 0
@@ -1825,7 +1900,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         pa.rank = rank;
         pa.c_old = c[cp];
         pa.c_new = c[1 - cp];
-        pa.sum = (T *)ws->pr_sum;
+        pa.sum = (Acc *)ws->pr_sum;
         pa.damping = REF ? 0.85 : p.damping;
         pa.acc = acc + 2 * cp;
         pa.dangling_prev = acc + 2 * (1 - cp) + 1;
@@ -1885,10 +1960,10 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         }
     }
     ASC_CUDA(cudaEventRecord(ws->ev[1], s));
-    if (out && !(p.flags & ASC_RUN_NO_OUTPUT))
-        ASC_CUDA(cudaMemcpyAsync(out, rank, sizeof(T) * (size_t)V,
-                                 (p.flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                 s));
+    if (out && !(p.flags & ASC_RUN_NO_OUTPUT)) {
+        ASC_TRY(copy_ranks_out<T>(g, rank, (void *)c[0], out, p.flags));
+        launches += sizeof(T) == 4;
+    }
     ASC_CUDA(cudaEventRecord(ws->ev[2], s));
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 6, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
@@ -2890,21 +2965,23 @@ asc_status run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint3
 // ------------------------------------------------- PageRank over CSR graphs --
 //
 // Graphs stored by out-edges (.bcsr / .bwcsr) run PageRank by scatter: every
-// vertex adds rank/outDeg to each out-neighbour's sum with an atomic add (FP32
-// or FP64 as asked), then one dense pass applies the update. The reference
-// PageRank semantics (per-vertex deactivation at |delta| <= 0.001, Jacobi
-// order) and the standard ones are the same as the pull kernels'; only the
-// summation order differs, as with any parallel sum.
+// vertex adds rank/outDeg to each out-neighbour's sum with an atomic add (FP64
+// contributions in FP64; FP32 contributions exactly, as the pull's 62-bit
+// fixed point, so an FP32 scatter's sums do not depend on the order of the
+// atomics), then one dense pass applies the update. The reference PageRank
+// semantics (per-vertex deactivation at |delta| <= 0.001, Jacobi order) and
+// the standard ones are the same as the pull kernels'.
 namespace {
 
 template <typename T>
 struct PushArgs {
+    typedef typename PrAcc<T>::type Acc;
     RegionArgs r0, r1;         // dense ranges and the fixed segment list
     const uint32_t *ptr;
-    T *rank;
+    double *rank;
     const T *c_old;
     T *c_new;
-    T *sum;
+    Acc *sum;
     uint32_t *active;          // reference mode: one bit per still-active vertex
     uint32_t *active_count;
     double damping;
@@ -2917,21 +2994,22 @@ template <typename T>
 struct PushSmem {
     uint32_t pref[kBlock + 1];
     uint32_t start[kBlock];
-    T c[kBlock];
+    typename PrAcc<T>::type c[kBlock];   // each tile vertex's contribution, as added
     uint32_t warp[kWarps + 1];
     uint32_t work;
 };
 
 template <typename T, int WORDS>
 __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t tile, PushSmem<T> &sm) {
+    typedef typename PrAcc<T>::type Acc;
     const uint32_t u = a.dense_begin + tile * kBlock + threadIdx.x;
     uint32_t deg = 0, start = 0;
-    T c = (T)0;
+    Acc c = (Acc)0;
     if (u < a.dense_end) {
         start = a.ptr[u];
         deg = a.ptr[u + 1] - start;
         if (deg > a.huge) deg = 0;
-        c = p.c_old[u];
+        c = PrAcc<T>::from(p.c_old[u]);
     }
     uint32_t total;
     const uint32_t excl = block_excl_scan(deg, total, sm.warp);
@@ -2942,12 +3020,12 @@ __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t ti
     __syncthreads();
     for (uint32_t base = 0; base < total; base += kUnroll * kBlock) {
         uint32_t v[kUnroll];
-        T ck[kUnroll];
+        Acc ck[kUnroll];
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const uint32_t e = base + k * kBlock + threadIdx.x;
             v[k] = 0xffffffffu;
-            ck[k] = (T)0;
+            ck[k] = (Acc)0;
             if (e < total) {
                 int lo = 0, hi = kBlock;
                 while (hi - lo > 1) {
@@ -2978,7 +3056,7 @@ __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t
     const uint64_t b = (uint64_t)a.ptr[u] + (uint64_t)k0 * a.seg_len;
     const uint64_t e = min((uint64_t)a.ptr[u + 1], b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
-    const T c = p.c_old[u];
+    const typename PrAcc<T>::type c = PrAcc<T>::from(p.c_old[u]);
     for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
         uint32_t v[kUnroll];
 #pragma unroll
@@ -3035,8 +3113,8 @@ __global__ void pr_push_apply_kernel(PushArgs<T> p, uint32_t V) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < V; base += stride) {
         const uint32_t v = base + threadIdx.x;
         if (v >= V) continue;
-        const T s = p.sum[v];
-        p.sum[v] = (T)0;
+        const double s = PrAcc<T>::value(p.sum[v]);
+        p.sum[v] = 0;
         const uint32_t od = p.ptr[v + 1] - p.ptr[v];
         if (REF) {
             const uint32_t bit = 1u << (v & 31);
@@ -3044,26 +3122,10 @@ __global__ void pr_push_apply_kernel(PushArgs<T> p, uint32_t V) {
                 p.c_new[v] = p.c_old[v];
                 continue;
             }
-            const double r = (double)p.rank[v];
-            const double t = fma(0.85, (double)s, 0.15);
-            const double diff = t > r ? t - r : r - t;
-            if (diff > 0.001) {
-                p.rank[v] = (T)t;
-                p.c_new[v] = od ? (T)(t / (double)od) : (T)0;
-                nact++;
-            } else {
-                atomicAnd(&p.active[v >> 5], ~bit);
-                p.c_new[v] = p.c_old[v];
-            }
+            if (pr_update<T>(p.rank, p.c_old, p.c_new, v, od, s, true, 0.85, (double)V, nullptr, res, dang)) nact++;
+            else atomicAnd(&p.active[v >> 5], ~bit);
         } else {
-            const double Vd = (double)V;
-            const T basev = (T)((1.0 - p.damping) / Vd + p.damping * (*p.dangling_prev) / Vd);
-            const T r = p.rank[v];
-            const T rn = basev + (T)p.damping * s;
-            res += fabs((double)rn - (double)r);
-            if (od == 0) dang += (double)rn;
-            p.rank[v] = rn;
-            p.c_new[v] = od ? rn / (T)od : (T)0;
+            pr_update<T>(p.rank, p.c_old, p.c_new, v, od, s, false, p.damping, (double)V, p.dangling_prev, res, dang);
         }
     }
     if (REF) {
@@ -3076,8 +3138,8 @@ __global__ void pr_push_apply_kernel(PushArgs<T> p, uint32_t V) {
 }
 
 template <typename T>
-__global__ void pr_push_init_kernel(T *rank, T *c0, T *c1, T *sum, const uint32_t *ptr, uint32_t *active, uint32_t V,
-                                    double *acc_pair) {
+__global__ void pr_push_init_kernel(double *rank, T *c0, T *c1, typename PrAcc<T>::type *sum, const uint32_t *ptr,
+                                    uint32_t *active, uint32_t V, double *acc_pair) {
     __shared__ double red[2 * kWarps];
     double d = 0;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -3086,12 +3148,12 @@ __global__ void pr_push_init_kernel(T *rank, T *c0, T *c1, T *sum, const uint32_
         if (i < V) {
             const double r = 1.0 / (double)V;
             const uint32_t od = ptr[i + 1] - ptr[i];
-            rank[i] = (T)r;
+            rank[i] = r;
             const T c = od ? (T)(r / (double)od) : (T)0;
             c0[i] = c;
             c1[i] = c;
-            sum[i] = (T)0;
-            if (od == 0) d += (double)(T)r;
+            sum[i] = 0;
+            if (od == 0) d += r;
         }
         if (i < (V + 31) / 32) active[i] = 0xffffffffu;
     }
@@ -3109,14 +3171,15 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
     uint32_t launches = 0;
     double *acc = (double *)(ws->ctl + CTL_PR);   // residual/dangling pairs by pass parity
     uint32_t *active_count = ws->ctl + CTL_PR + 8;  // word 40
-    T *rank = (T *)ws->pr_rank;
+    typedef typename PrAcc<T>::type Acc;
+    double *rank = (double *)ws->pr_rank;
     T *c[2] = {(T *)ws->pr_contrib[0], (T *)ws->pr_contrib[1]};
     uint32_t *active = ws->bitmap[1];
 
     ASC_CUDA(cudaEventRecord(ws->ev[0], s));
     ASC_CUDA(cudaMemsetAsync(ws->ctl, 0, 4 * CTL_WORDS, s));
-    pr_push_init_kernel<T><<<fill_grid(ws, V), kBlock, 0, s>>>(rank, c[0], c[1], (T *)ws->pr_sum, g->d_ptr, active, V,
-                                                               acc + 2);
+    pr_push_init_kernel<T><<<fill_grid(ws, V), kBlock, 0, s>>>(rank, c[0], c[1], (Acc *)ws->pr_sum, g->d_ptr, active,
+                                                               V, acc + 2);
     launches++;
     if (ws->n_huge_total) {
         seed_huge_segments_kernel<<<fill_grid(ws, ws->n_huge_total), kBlock, 0, s>>>(
@@ -3145,7 +3208,7 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
         pa.rank = rank;
         pa.c_old = c[cp];
         pa.c_new = c[1 - cp];
-        pa.sum = (T *)ws->pr_sum;
+        pa.sum = (Acc *)ws->pr_sum;
         pa.active = active;
         pa.active_count = active_count;
         pa.damping = REF ? 0.85 : p.damping;
@@ -3167,10 +3230,10 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
         }
     }
     ASC_CUDA(cudaEventRecord(ws->ev[1], s));
-    if (out && !(p.flags & ASC_RUN_NO_OUTPUT))
-        ASC_CUDA(cudaMemcpyAsync(out, rank, sizeof(T) * (size_t)V,
-                                 (p.flags & ASC_RUN_DEVICE_OUT) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                 s));
+    if (out && !(p.flags & ASC_RUN_NO_OUTPUT)) {
+        ASC_TRY(copy_ranks_out<T>(g, rank, (void *)c[0], out, p.flags));
+        launches += sizeof(T) == 4;
+    }
     ASC_CUDA(cudaEventRecord(ws->ev[2], s));
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 8 * 4, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
@@ -3407,7 +3470,9 @@ constexpr uint64_t kNaBytes = na_round(kNaSegs1 + 8 * kNoAllocMaxSegs);   // abo
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 // In host code g_noalloc_scratch names a host-side stand-in, not device memory;
-// kernels get the device address looked up once per device.
+// kernels get the device address looked up once per device. The cached address
+// belongs to the device's primary context: a cudaDeviceReset or another context
+// would leave it stale, which the header rules out for callers.
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mutex;
 unsigned char *g_na_addr[kNaMaxDevices] = {nullptr};

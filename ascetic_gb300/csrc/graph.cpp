@@ -202,22 +202,23 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : eb;  // budget unit
     uint64_t frag = b->fragment_edges ? b->fragment_edges : 4096;
     uint64_t st = E;
-    bool round_down = false;
+    // every capped mode ends in the reference's rule (GraphMeta.cuh:341-353):
+    // the cap in edges, at most E and 2^32 - 1, rounded down to whole fragments
+    bool round_down = true;
     switch (b->mode) {
         case ASC_BUDGET_ALL:
             st = E;
+            round_down = false;
             break;
         case ASC_BUDGET_FRAC:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget fraction %g is negative", b->value);
             // the fraction of the source edge-array bytes, spent on device-format edges
             if (b->value * fb >= eb) st = E;
-            else { st = (uint64_t)(b->value * (double)E * fb / eb); round_down = true; }
+            else st = (uint64_t)(b->value * (double)E * fb / eb);
             break;
         case ASC_BUDGET_BYTES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget bytes %g is negative", b->value);
-            st = (uint64_t)(b->value / eb);
-            if (st >= E) st = E;
-            else round_down = true;
+            st = b->value / eb >= (double)E ? E : (uint64_t)(b->value / eb);
             break;
         case ASC_BUDGET_ADVISE_K: {
             // GraphMeta.cuh:318-354, in 64-bit arithmetic (the reference keeps
@@ -234,22 +235,24 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
                 if (k > 1) k = 1.0;
             }
             st = (uint64_t)((float)k * (double)total_edges);
-            if (st > E) st = E;
-            if (st > kU32Max) st = kU32Max;
-            round_down = true;
             break;
         }
         case ASC_BUDGET_EDGES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget edges %g is negative", b->value);
-            st = std::min<uint64_t>(E, (uint64_t)b->value);
+            st = b->value >= (double)E ? E : (uint64_t)b->value;
             break;
         case ASC_BUDGET_MANAGED:
             st = 0;
+            round_down = false;
             break;
         default:
             return fail(ASC_ERR_INVALID, "unknown budget mode %u", b->mode);
     }
-    if (round_down) st -= st % frag;
+    if (round_down) {
+        if (st > E) st = E;
+        if (st > kU32Max) st = kU32Max;
+        st -= st % frag;
+    }
     g->static_edges = st;
     // S = number of leading vertices whose whole list lies in [0, st); offsets
     // never decrease, so the static vertices are a prefix of the ids.

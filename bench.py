@@ -57,12 +57,17 @@ def parse():
                     help="profiling aid: time the steps with one launch per region (phase timing)")
     ap.add_argument("--batch", type=int, default=64,
                     help="sources of the multi-source leg (0 skips it)")
-    ap.add_argument("--serve", default="16,18,20,22",
-                    help="RMAT scales of the resident graphs of the serving leg ('' skips it); "
-                         "20,22,24,26 is the full serving configuration")
-    ap.add_argument("--serve-queries", type=int, default=400)
+    ap.add_argument("--serve", default="20,22,24,26",
+                    help="RMAT scales of the resident graphs of the serving leg ('' skips it)")
+    ap.add_argument("--serve-queries", type=int, default=10000, help="queries of the serving stream")
+    ap.add_argument("--serve-fifo-queries", type=int, default=1000,
+                    help="prefix of the stream the plain FIFO engine serves under saturating load")
     ap.add_argument("--serve-budget-gb", type=float, default=12.0)
     ap.add_argument("--serve-sweep", type=int, default=1, help="run the Poisson rate sweep (0 skips it)")
+    ap.add_argument("--serve-sweep-queries", type=int, default=1000,
+                    help="queries per rate of the batched server's Poisson sweep")
+    ap.add_argument("--serve-sweep-fifo-queries", type=int, default=300,
+                    help="queries of both servers at half the plain engine's capacity")
     ap.add_argument("--pr-study", type=int, default=0,
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
@@ -207,11 +212,12 @@ def pr_study(args):
             r, st = g.run("pr", params=prm)
             res[name] = (r.astype(np.float64), st)
     t1 = time.perf_counter()
-    exact, it, resid = oracle.pr_std(cptr, ccol, od)
+    exact, it, resid = oracle.pr_std_mt(cptr, ccol, od, oracle_threads())
     oracle_s = time.perf_counter() - t1
     for name, (r, st) in res.items():
         out[name] = {"ms": round(st["ms_total"], 2), "passes": st["iterations"], "residual": st["residual"],
                      "max_abs_err_vs_fp64_oracle": float(np.abs(r - exact).max()),
+                     "max_rel_err_vs_fp64_oracle": float((np.abs(r - exact) / exact).max()),
                      "l1_err_vs_fp64_oracle": float(np.abs(r - exact).sum()),
                      "ondemand_bytes": st["ondemand_bytes"]}
     # FP32 pass time against the static fraction: every edge in HBM (the pull's
@@ -227,7 +233,7 @@ def pr_study(args):
                                     "ondemand_gbps": round(st["ondemand_bytes"] / (st["ms_total"] * 1e-3) / 1e9, 1)}
     out["fp32_pass_by_budget"] = by_budget
     out["fp32_vs_fp64_gpu_max_abs"] = float(np.abs(res["fp32"][0] - res["fp64"][0]).max())
-    out["oracle"] = {"passes": it, "residual": resid, "seconds_1_core": round(oracle_s, 1)}
+    out["oracle"] = {"passes": it, "residual": resid, "seconds": round(oracle_s, 1), "threads": oracle_threads()}
     out["within_1e-6"] = bool(out["fp32"]["max_abs_err_vs_fp64_oracle"] <= 1e-6)
     print(json.dumps(out), flush=True)
 
@@ -236,40 +242,61 @@ def serve_leg(args):
     """Serving: BFS/SSSP/CC/PR queries (mix 50/30/10/10, graph uniform, sources
     uniform over vertices with out-degree > 0) against resident RMAT graphs
     (edge factor 16, seeds 5.., weights uniform in [1,63], static region 25% of
-    edge bytes) under one device budget. The continuous-batching server against
-    the plain one-query-at-a-time FIFO engine on the same GPU: saturating load
-    (all queries submitted at once), then Poisson arrivals at swept rates."""
+    each graph's edge bytes) under one device budget that covers every device
+    allocation. The continuous-batching server against the plain
+    one-query-at-a-time FIFO engine on the same GPU: saturating load (the whole
+    stream submitted at once; the FIFO engine gets a stated prefix of the same
+    stream), then Poisson arrivals at swept rates.
+
+    Every query's values are copied out to host memory. Queries outside the
+    checked sample share one host buffer per graph and value type (the copy
+    happens, the values are overwritten); the sample (spread over the stream,
+    every graph and algorithm) keeps its own buffers, and its BFS/SSSP/CC
+    values must equal the plain engine's bit for bit, PageRank within 1e-6."""
     import ascetic_gb300 as A
     scales = [int(x) for x in args.serve.split(",") if x]
     rng = np.random.default_rng(12345)
-    graphs, cands, hosts = [], [], []
+    graphs, cands = [], []
     t0 = time.time()
     for i, sc in enumerate(scales):
         ptr, adj = A.rmat_csr(sc, 16, 5 + i, weights=(1, 63))
         deg = np.diff(ptr)
         cands.append(np.nonzero(deg > 0)[0])
         graphs.append(A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=args.budget)))
-        hosts.append((ptr, adj) if sc <= 20 else None)
-        del ptr, adj
+        del ptr, adj, deg
     t_gen = time.time() - t0
     std32 = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
     plan = []
     for _ in range(args.serve_queries):
         gi = int(rng.integers(0, len(scales)))
         r = rng.random()
-        if r < 0.5:
-            algo = "bfs"
-        elif r < 0.8:
-            algo = "sssp"
-        elif r < 0.9:
-            algo = "cc"
-        else:
-            algo = "pr"
+        algo = "bfs" if r < 0.5 else ("sssp" if r < 0.8 else ("cc" if r < 0.9 else "pr"))
         src = int(rng.choice(cands[gi])) if algo in ("bfs", "sssp") else 0
         plan.append((gi, algo, src))
+    n_fifo = min(len(plan), args.serve_fifo_queries)
+    # checked sample: every k-th query of the FIFO prefix, plus the first query
+    # of each (graph, algorithm) pair there
+    step = max(1, n_fifo // 48)
+    sample = set(range(0, n_fifo, step))
+    seen = set()
+    for k, (gi, algo, _) in enumerate(plan[:n_fifo]):
+        if (gi, algo) not in seen:
+            seen.add((gi, algo))
+            sample.add(k)
+    sinks = {}
+
+    def out_for(k, gi, algo):
+        dt = np.float32 if algo == "pr" else np.uint32
+        if k in sample:
+            return np.empty(graphs[gi].V, dt)
+        key = (gi, dt)
+        if key not in sinks:
+            sinks[key] = np.empty(graphs[gi].V, dt)
+        return sinks[key]
+
     budget = int(args.serve_budget_gb * 1e9)
 
-    def run(mode, rate=None, n=None):
+    def run(mode, rate=None, n=None, keep=False):
         todo = plan if n is None else plan[:n]
         with A.Server(budget_bytes=budget, mode=mode) as srv:
             ids = [srv.add_graph(g) for g in graphs]
@@ -281,40 +308,57 @@ def serve_leg(args):
                     delay = t_start + arr[k] - time.perf_counter()
                     if delay > 0:
                         time.sleep(delay)
-                tick.append(srv.submit(ids[gi], algo, src, params=std32 if algo == "pr" else None))
-            outs = [srv.wait(t) for t in tick]
+                tick.append(srv.submit(ids[gi], algo, src, params=std32 if algo == "pr" else None,
+                                       out=out_for(k, gi, algo)))
+            kept = {}
+            for k, t in enumerate(tick):
+                o, _ = srv.wait(t)
+                if keep and k in sample:
+                    kept[k] = o
             st = srv.stats()
-        return st, outs
+            wall = time.perf_counter() - t_start
+        return st, kept, wall
 
     # warm-up (graph loops, batch state) then saturating load
     run(A.SERVE_BATCHED, n=min(40, len(plan)))
     run(A.SERVE_FIFO, n=min(8, len(plan)))
-    sb, outs_b = run(A.SERVE_BATCHED)
-    sf, outs_f = run(A.SERVE_FIFO)
-    # every served BFS/SSSP/CC value equals the plain engine's (bit for bit)
-    exact = True
-    for (gi, algo, src), (ob, _), (of, _) in zip(plan, outs_b, outs_f):
-        if algo != "pr" and not np.array_equal(ob, of):
+    sb, kb, wb = run(A.SERVE_BATCHED, keep=True)
+    sf, kf, wf = run(A.SERVE_FIFO, n=n_fifo, keep=True)
+    exact, pr_err = True, 0.0
+    for k in sorted(sample):
+        algo = plan[k][1]
+        if algo == "pr":
+            pr_err = max(pr_err, float(np.abs(kb[k].astype(np.float64) - kf[k].astype(np.float64)).max()))
+        elif not np.array_equal(kb[k], kf[k]):
             exact = False
-            break
+    del kb, kf
     res = {"graphs_rmat_scales": scales, "queries": len(plan), "mix": "50% BFS / 30% SSSP / 10% CC / 10% PR (FP32)",
            "budget_bytes": budget, "graph_build_s": round(t_gen, 1),
            "batched": {"qps": round(sb["queries_per_s"], 2), "p50_ms": round(sb["p50_ms"], 2),
-                       "p99_ms": round(sb["p99_ms"], 2), "device_bytes": sb["device_bytes"]},
+                       "p99_ms": round(sb["p99_ms"], 2), "device_bytes": sb["device_bytes"],
+                       "queries": len(plan), "wall_s": round(wb, 1)},
            "plain_fifo": {"qps": round(sf["queries_per_s"], 2), "p50_ms": round(sf["p50_ms"], 2),
-                          "p99_ms": round(sf["p99_ms"], 2)},
+                          "p99_ms": round(sf["p99_ms"], 2), "queries": n_fifo, "wall_s": round(wf, 1),
+                          "note": "the first %d queries of the same stream" % n_fifo},
            "qps_speedup": round(sb["queries_per_s"] / sf["queries_per_s"], 2) if sf["queries_per_s"] else None,
-           "results_equal_plain_engine": bool(exact), "load": "saturating (all submitted at t=0)"}
+           "checked_queries": len(sample), "results_equal_plain_engine": bool(exact),
+           "pagerank_max_abs_vs_plain_engine": pr_err, "load": "saturating (all submitted at t=0)"}
     sweep = []
-    cap = sf["queries_per_s"]
-    n_sweep = min(len(plan), 120)
-    for frac in ((0.5, 0.9, 2.0) if args.serve_sweep else ()):
-        rate = frac * cap
-        b, _ = run(A.SERVE_BATCHED, rate=rate, n=n_sweep)
-        f, _ = run(A.SERVE_FIFO, rate=rate, n=n_sweep)
-        sweep.append({"rate_qps": round(rate, 2), "batched_p50_ms": round(b["p50_ms"], 2),
-                      "batched_p99_ms": round(b["p99_ms"], 2), "fifo_p50_ms": round(f["p50_ms"], 2),
-                      "fifo_p99_ms": round(f["p99_ms"], 2), "queries": n_sweep})
+    cap_b, cap_f = sb["queries_per_s"], sf["queries_per_s"]
+    if args.serve_sweep:
+        for frac in (0.25, 0.5, 0.9):
+            rate = frac * cap_b
+            b, _, _ = run(A.SERVE_BATCHED, rate=rate, n=min(len(plan), args.serve_sweep_queries))
+            sweep.append({"server": "batched", "rate_qps": round(rate, 2), "rate_frac_of_batched_capacity": frac,
+                          "p50_ms": round(b["p50_ms"], 2), "p99_ms": round(b["p99_ms"], 2),
+                          "queries": min(len(plan), args.serve_sweep_queries)})
+        # both servers at a rate the plain engine can sustain (half its capacity)
+        rate = 0.5 * cap_f
+        n_low = min(len(plan), args.serve_sweep_fifo_queries)
+        for name, mode in (("batched", A.SERVE_BATCHED), ("plain_fifo", A.SERVE_FIFO)):
+            b, _, _ = run(mode, rate=rate, n=n_low)
+            sweep.append({"server": name, "rate_qps": round(rate, 2), "rate_frac_of_fifo_capacity": 0.5,
+                          "p50_ms": round(b["p50_ms"], 2), "p99_ms": round(b["p99_ms"], 2), "queries": n_low})
     res["poisson_sweep"] = sweep
     for g in graphs:
         g.close()
@@ -580,9 +624,28 @@ def replica_reduce(edges, seconds, world):
     return e.item(), t.item()
 
 
-def batch_bfs_leg(A, g, ptr, args):
+def oracle_threads():
+    return os.cpu_count() or 1
+
+
+def check_rows(mode, ptr, edges, sources, rows):
+    """Rows of engine results against the oracle's run of the reference
+    frontier scheme on all host threads (oracle.relax_mt: BFS, SSSP and CC have
+    one fixpoint each, so any correct schedule gives these exact values).
+    Returns (all bit-exact, oracle seconds)."""
+    import oracle
+    t = time.perf_counter()
+    ok = True
+    for s_, row in zip(sources, rows):
+        exp, _ = oracle.relax_mt(mode, ptr, edges, s_, oracle_threads())
+        ok = ok and bool(np.array_equal(np.asarray(row), exp))
+    return ok, time.perf_counter() - t
+
+
+def batch_bfs_leg(A, g, ptr, col, args):
     """One batch of up to 64 BFS sources against the same sources one at a
-    time, and rows of a 4-source batch checked against single runs."""
+    time; four rows of that batch (first, last and two between) checked
+    against the oracle."""
     bsrc = pick_sources(ptr, args.batch, args.seed + 100)
     # warm-up: the same batch once (its launches are the ones to profile)
     g.run_batch("bfs", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
@@ -592,25 +655,27 @@ def batch_bfs_leg(A, g, ptr, args):
         _, st = g.run("bfs", s_, params=A.make_params(flags=A.RUN_NO_OUTPUT))
         seq_ms += st["ms_total"]
         seq_edges += st["reached_edges"]
-    rows, _ = g.run_batch("bfs", bsrc[:4])
-    exact = all(np.array_equal(rows[i], g.run("bfs", s_)[0]) for i, s_ in enumerate(bsrc[:4]))
+    rows, _ = g.run_batch("bfs", bsrc)
+    chk = sorted({0, len(bsrc) // 3, 2 * len(bsrc) // 3, len(bsrc) - 1})
+    kept = [rows[i].copy() for i in chk]
+    del rows
+    exact, oracle_s = check_rows(0, ptr, col, [bsrc[i] for i in chk], kept)
     return {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
             "sequential_ms": round(seq_ms, 3),
             "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
             "batch_gteps": round(seq_edges / (bst["ms_total"] * 1e-3) / 1e9, 3),
             "ondemand_bytes": bst["ondemand_bytes"], "iterations": bst["iterations"],
-            "rows_checked_bit_exact": 4, "bit_exact": bool(exact)}
+            "rows_checked_vs_oracle": chk, "bit_exact": bool(exact), "oracle_s": round(oracle_s, 1)}
 
 
 def batch_sssp_leg(A, ptr, budget, args):
     """One batch of up to 64 SSSP sources (weights uniform in [1, 63]) against
     the same sources one at a time; rows of the full batch (its many-source
-    relaxation path) checked against single runs when the rows fit in 8 GB of
+    relaxation path) checked against the oracle when the rows fit in 8 GB of
     host memory, else rows of a 4-source batch."""
     V = len(ptr) - 1
-    _, adjb = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
-    with A.Graph.from_csr(ptr, adjb, budget=budget) as gw:
-        del adjb
+    _, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
+    with A.Graph.from_csr(ptr, adj, budget=budget) as gw:
         bsrc = pick_sources(ptr, args.batch, args.seed + 200)
         # warm-up: the same batch once (its launches are the ones to profile)
         gw.run_batch("sssp", bsrc, params=A.make_params(flags=A.RUN_NO_OUTPUT))
@@ -625,14 +690,15 @@ def batch_sssp_leg(A, ptr, budget, args):
         else:
             rows, _ = gw.run_batch("sssp", bsrc[:4])
             chk = list(range(min(4, len(bsrc))))
-        exact = all(np.array_equal(rows[i], gw.run("sssp", bsrc[i])[0]) for i in chk)
+        kept = [rows[i].copy() for i in chk]
         del rows
-        return {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
-                "sequential_ms": round(seq_ms, 3),
-                "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
-                "iterations": bst["iterations"], "edges_processed": bst["edges_processed"],
-                "ondemand_bytes": bst["ondemand_bytes"], "rows_checked_bit_exact": chk,
-                "bit_exact": bool(exact)}
+    exact, oracle_s = check_rows(1, ptr, adj, [bsrc[i] for i in chk], kept)
+    return {"sources": len(bsrc), "batch_ms": round(bst["ms_total"], 3),
+            "sequential_ms": round(seq_ms, 3),
+            "speedup": round(seq_ms / bst["ms_total"], 2) if bst["ms_total"] else None,
+            "iterations": bst["iterations"], "edges_processed": bst["edges_processed"],
+            "ondemand_bytes": bst["ondemand_bytes"], "rows_checked_vs_oracle": chk,
+            "bit_exact": bool(exact), "oracle_s": round(oracle_s, 1)}
 
 
 def batch_study(args):
@@ -646,7 +712,7 @@ def batch_study(args):
     out = {"study": "multi-source batches vs the same sources one at a time", "rmat_scale": args.scale,
            "budget_frac": args.budget}
     with A.Graph.from_csr(ptr, col, budget=budget) as g:
-        out["batch_bfs"] = batch_bfs_leg(A, g, ptr, args)
+        out["batch_bfs"] = batch_bfs_leg(A, g, ptr, col, args)
     del col
     out["batch_sssp"] = batch_sssp_leg(A, ptr, budget, args)
     print(json.dumps(out), flush=True)
@@ -796,6 +862,15 @@ def main():
     roofline = dict(roofline)
     roofline["dominant"] = dominant
 
+    # parity of the timed workload: the levels of every timed source (run again
+    # with output, after the timed region) against the oracle
+    parity = {"oracle": "oracle.relax_mt: the reference's frontier/atomic-min scheme on %d host threads "
+                        "(BFS, SSSP and CC have one fixpoint each)" % oracle_threads()}
+    lv = [g.run("bfs", s_)[0] for s_ in srcs]
+    ok, o_s = check_rows(0, ptr, col, srcs, lv)
+    del lv
+    parity["bfs"] = {"sources": len(srcs), "bit_exact": ok, "oracle_s": round(o_s, 1)}
+
     line = {"metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(tot_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic RMAT (seeded)",
@@ -809,7 +884,9 @@ def main():
                       "generate_s": round(t_gen, 2)},
             "host_wall_ms_per_step": round(1e3 * t_wall / args.steps, 3)}
     if args.batch:
-        line["batch_bfs"] = batch_bfs_leg(A, g, ptr, args)
+        line["batch_bfs"] = batch_bfs_leg(A, g, ptr, col, args)
+        parity["batch_bfs_rows"] = {"rows": line["batch_bfs"]["rows_checked_vs_oracle"],
+                                    "bit_exact": line["batch_bfs"]["bit_exact"]}
     g.close()
     if args.batch and args.batch_sssp:
         line["batch_sssp"] = batch_sssp_leg(A, ptr, budget, args)
@@ -833,7 +910,10 @@ def main():
             extra["sssp_processed_per_reached_edge"] = round(proc / e, 3) if e else None
             extra["sssp_iterations"] = its / 4
             extra["sssp_tuning"] = gw.get_tuning()
-        del adj
+            dist = [gw.run("sssp", s_)[0] for s_ in srcs[:4]]
+        ok, o_s = check_rows(1, ptr, adj, srcs[:4], dist)
+        parity["sssp"] = {"sources": 4, "bit_exact": ok, "oracle_s": round(o_s, 1)}
+        del adj, dist
         sp, sc = A.rmat_csr(args.scale, args.edge_factor, args.seed, symmetric=True)
         with A.Graph.from_csr(sp, sc, budget=budget) as gs:
             if not args.no_tune:
@@ -844,7 +924,10 @@ def main():
             extra["cc_ms"] = round(st["ms_total"], 3)
             extra["cc_processed_edges_per_s_G"] = round(st["edges_processed"] / (st["ms_total"] * 1e-3) / 1e9, 4)
             extra["cc_iterations"] = st["iterations"]
-        del sp, sc
+            labels = gs.run("cc")[0]
+        ok, o_s = check_rows(2, sp, sc, [0], [labels])
+        parity["cc"] = {"bit_exact": ok, "oracle_s": round(o_s, 1)}
+        del sp, sc, labels
         line["other_algorithms"] = extra
 
     if args.serve:
@@ -859,6 +942,8 @@ def main():
         line["cpu_baseline"] = {"value": round(re / dt / 1e9, 4), "unit": "GTEPS", "cores": 1, "kind": "port",
                                 "sample": "one serial queue BFS (oracle orc_bfs) from source %d of the same graph, "
                                           "%.2f s" % (srcs[0], dt)}
+    parity["all_bit_exact"] = all(v["bit_exact"] for v in parity.values() if isinstance(v, dict))
+    line["parity"] = parity
     if world > 1:
         line["config"]["parallelism"] = "%d independent replicas (the path does not shard)" % world
     print(json.dumps(line), flush=True)

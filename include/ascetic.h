@@ -63,13 +63,18 @@ typedef enum asc_format {
 typedef enum asc_algo { ASC_BFS = 0, ASC_SSSP = 1, ASC_CC = 2, ASC_PR = 3 } asc_algo;
 
 typedef enum asc_budget_mode {
-    ASC_BUDGET_ALL = 0,      /* whole edge array resident (no cap) */
+    /* Every mode but ALL and MANAGED gives a cap in edges that ends in the
+     * reference's rule (GraphMeta.cuh:341-365): at most E and 2^32 - 1, rounded
+     * down to whole fragments (fragment_edges, default 4096, as the reference's
+     * fragmentSize), so the same cap puts the same prefix on the device. */
+    ASC_BUDGET_ALL = 0,      /* whole edge array resident (no cap, no rounding) */
     ASC_BUDGET_FRAC = 1,     /* value = fraction of the source edge-array bytes (4 or 8 per edge as in
                                 the file) for the static region */
     ASC_BUDGET_BYTES = 2,    /* value = bytes for the static region */
     ASC_BUDGET_ADVISE_K = 3, /* value = reference --adviseK: fraction of free device memory left
                                 after the vertex arrays (GraphMeta.cuh:310-354); 0 = its auto formula */
-    ASC_BUDGET_EDGES = 4,    /* value = exact static edge count (no fragment rounding) */
+    ASC_BUDGET_EDGES = 4,    /* value = static edge cap (the reference's max_partition_size before
+                                its rounding) */
     ASC_BUDGET_MANAGED = 5   /* comparison engine, the reference's UVM baseline (bfs.cu:249-273): no
                                 static region; the edge array lives in CUDA managed memory advised
                                 read-mostly and the driver copies pages to the GPU as kernels touch
@@ -365,7 +370,14 @@ asc_status asc_link_probe_runs(uint64_t bytes, uint32_t run_bytes, int iters, do
  * every GPU that loads it until the process exits; no cudaMalloc, cudaFree or
  * allocating library routine is called. The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current, so
- * make that first call before any stream capture. All calls share the array
+ * make that first call before any stream capture. The address is kept for the
+ * life of the process, so it assumes the device's primary context does too:
+ * after a cudaDeviceReset, or from a context other than the primary one, the
+ * kept address is stale and the entry point must not be called. The array is
+ * committed on a device when this library's device code is loaded there (with
+ * lazy module loading, at the first call into the library that uses that
+ * device): a caller whose own allocator will later reserve the rest of the
+ * device makes one warm-up call before it does. All calls share the array
  * (counters are cleared at the start of each call): calls that overlap on the
  * GPU, on any stream or thread, race and must not be issued. */
 asc_status asc_bfs_device_noalloc(uint64_t V, uint64_t E, const uint32_t *d_row_offsets, const uint32_t *d_col,

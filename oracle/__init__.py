@@ -63,11 +63,13 @@ def _load():
     lib.orc_pr_ref.argtypes = [u64, _u64p, _u32p, _u32p, _f64p, i32p]
     lib.orc_pr_std.argtypes = [u64, _u64p, _u32p, _u32p, ctypes.c_double, ctypes.c_double,
                                ctypes.c_int32, _f64p, i32p, ctypes.POINTER(ctypes.c_double)]
+    lib.orc_pr_std_mt.argtypes = [u64, _u64p, _u32p, _u32p, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_int32, ctypes.c_int, _f64p, i32p, ctypes.POINTER(ctypes.c_double)]
     lib.orc_static_split.argtypes = [u64, _u64p, u64, _u8p, ctypes.POINTER(u64), ctypes.POINTER(u64)]
     lib.orc_reached_edges.argtypes = [u64, _u64p, _u32p, u32]
     lib.orc_reached_edges.restype = u64
     lib.orc_relax_mt.argtypes = [ctypes.c_int, u64, _u64p, _u32p, u32, ctypes.c_int, _u32p, i32p]
-    for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pr_ref", "orc_pr_std", "orc_static_split",
+    for f in ("orc_bfs", "orc_sssp", "orc_cc", "orc_pr_ref", "orc_pr_std", "orc_pr_std_mt", "orc_static_split",
               "orc_relax_mt"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
@@ -134,6 +136,21 @@ def pr_std(ptr, col, outdeg, damping=0.85, tol=1e-9, max_iter=100):
                               damping, tol, max_iter, out, ctypes.byref(it), ctypes.byref(res)),
            "pr_std")
     return out, it.value, res.value
+
+
+def pr_std_mt(ptr, col, outdeg, nthreads, damping=0.85, tol=1e-9, max_iter=100):
+    """pr_std on host threads (same per-vertex sums; the dangling mass and the
+    residual are combined from per-thread partials); returns (ranks, passes,
+    l1_residual)."""
+    ptr, col, outdeg = _ptr(ptr), _u32(col), _u32(outdeg)
+    V = len(ptr) - 1
+    out = np.empty(max(V, 1), np.float64)
+    it = ctypes.c_int32(0)
+    res = ctypes.c_double(0)
+    _check(_load().orc_pr_std_mt(V, ptr, col if len(col) else np.zeros(1, np.uint32), outdeg,
+                                 damping, tol, max_iter, int(nthreads), out, ctypes.byref(it), ctypes.byref(res)),
+           "pr_std_mt")
+    return out[:V], it.value, res.value
 
 
 def static_split(ptr, static_edges_cap):

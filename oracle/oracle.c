@@ -258,6 +258,87 @@ int orc_pr_std(uint64_t V, const uint64_t *ptr, const uint32_t *col, const uint3
     return ORC_OK;
 }
 
+/* orc_pr_std on host threads, for graphs where one core takes minutes: each
+ * pass computes the contributions (and per-thread dangling partials), then
+ * every vertex's sum over its in-edges serially in CSC order exactly as
+ * orc_pr_std (and per-thread residual partials). Partials are combined in
+ * thread order, so a run is deterministic for a thread count; the dangling
+ * mass and residual differ from the serial sums only in rounding order. */
+typedef struct {
+    int phase;
+    uint64_t lo, hi;
+    const uint64_t *ptr;
+    const uint32_t *col;
+    const uint32_t *outdeg;
+    const double *rank;
+    double *nxt, *contrib;
+    double base, damping, part;
+} pr_job;
+
+static void *pr_worker(void *arg)
+{
+    pr_job *j = (pr_job *)arg;
+    double acc = 0;
+    if (j->phase == 0) {
+        for (uint64_t u = j->lo; u < j->hi; u++) {
+            if (j->outdeg[u] == 0) { acc += j->rank[u]; j->contrib[u] = 0; }
+            else j->contrib[u] = j->rank[u] / (double)j->outdeg[u];
+        }
+    } else {
+        for (uint64_t v = j->lo; v < j->hi; v++) {
+            double s = 0;
+            for (uint64_t k = j->ptr[v]; k < j->ptr[v + 1]; k++) s += j->contrib[j->col[k]];
+            double r = j->base + j->damping * s;
+            acc += fabs(r - j->rank[v]);
+            j->nxt[v] = r;
+        }
+    }
+    j->part = acc;
+    return NULL;
+}
+
+int orc_pr_std_mt(uint64_t V, const uint64_t *ptr, const uint32_t *col, const uint32_t *outdeg,
+                  double damping, double tol, int32_t max_iter, int nthreads,
+                  double *rank, int32_t *iters_out, double *residual_out)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (V == 0) { if (iters_out) *iters_out = 0; if (residual_out) *residual_out = 0; return ORC_OK; }
+    double *nxt = (double *)malloc(sizeof(double) * V);
+    double *contrib = (double *)malloc(sizeof(double) * V);
+    pr_job *jobs = (pr_job *)calloc((size_t)nthreads, sizeof(pr_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!nxt || !contrib || !jobs || !th) { free(nxt); free(contrib); free(jobs); free(th); return ORC_ERR_MEM; }
+    double inv_v = 1.0 / (double)V;
+    for (uint64_t i = 0; i < V; i++) rank[i] = inv_v;
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].lo = V * (uint64_t)t / (uint64_t)nthreads;
+        jobs[t].hi = V * (uint64_t)(t + 1) / (uint64_t)nthreads;
+        jobs[t].ptr = ptr; jobs[t].col = col; jobs[t].outdeg = outdeg;
+        jobs[t].rank = rank; jobs[t].nxt = nxt; jobs[t].contrib = contrib; jobs[t].damping = damping;
+    }
+    int32_t it = 0;
+    double res = 0;
+    while (it < max_iter) {
+        double sums[2] = {0, 0};
+        for (int phase = 0; phase < 2; phase++) {
+            double base = (1.0 - damping) * inv_v + damping * sums[0] * inv_v;
+            for (int t = 0; t < nthreads; t++) { jobs[t].phase = phase; jobs[t].base = base; }
+            for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, pr_worker, &jobs[t]);
+            pr_worker(&jobs[0]);
+            for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+            for (int t = 0; t < nthreads; t++) sums[phase] += jobs[t].part;
+        }
+        res = sums[1];
+        memcpy(rank, nxt, sizeof(double) * V);
+        it++;
+        if (res < tol) break;
+    }
+    free(nxt); free(contrib); free(jobs); free(th);
+    if (iters_out) *iters_out = it;
+    if (residual_out) *residual_out = res;
+    return ORC_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Static/on-demand split (GraphMeta.cuh:341-372): the static region is the
  * prefix edge[0, mps) of the edge array with mps rounded down to a multiple of

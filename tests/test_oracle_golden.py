@@ -72,6 +72,15 @@ def test_pr_std_converges_and_sums_to_one():
     assert res < 1e-9 and it < 100
 
 
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_threaded_pr_std_matches_serial(threads):
+    z = np.load(os.path.join(GOLDEN, "rmat_s11_ef8_seed2.npz"))
+    r, it, res = oracle.pr_std(z["cptr"], z["ccol"], z["outdeg"])
+    r2, it2, res2 = oracle.pr_std_mt(z["cptr"], z["ccol"], z["outdeg"], threads)
+    assert it2 == it and abs(res2 - res) <= 1e-15
+    assert np.abs(r2 - r).max() <= 1e-15
+
+
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_threaded_reference_scheme_matches_oracle(mode):
     z = np.load(os.path.join(GOLDEN, "rmat_s11_ef8_seed2.npz"))
