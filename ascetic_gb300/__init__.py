@@ -32,6 +32,7 @@ BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES, BUDGET_MAN
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
 RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP, RUN_FRAGMENT_COUNTS, RUN_GATHER_COPY = 1, 2, 4, 8, 16, 32
+RUN_NO_STAGING = 64
 RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 
@@ -60,7 +61,8 @@ class AscError(RuntimeError):
 
 
 class Budget(ctypes.Structure):
-    _fields_ = [("mode", ctypes.c_uint32), ("fragment_edges", ctypes.c_uint32), ("value", ctypes.c_double)]
+    _fields_ = [("mode", ctypes.c_uint32), ("fragment_edges", ctypes.c_uint32), ("value", ctypes.c_double),
+                ("stage_bytes", ctypes.c_uint64)]
 
 
 class GraphInfo(ctypes.Structure):
@@ -69,16 +71,17 @@ class GraphInfo(ctypes.Structure):
                 ("static_vertices", ctypes.c_uint64), ("device_edge_bytes", ctypes.c_uint64),
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
                 ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32),
-                ("weight_bits", ctypes.c_uint32), ("edge_bits", ctypes.c_uint32)]
+                ("weight_bits", ctypes.c_uint32), ("edge_bits", ctypes.c_uint32),
+                ("staging_bytes", ctypes.c_uint64)]
 
 
 class Tuning(ctypes.Structure):
     _fields_ = [("huge_degree", ctypes.c_uint32), ("segment_edges", ctypes.c_uint32),
                 ("dense_div", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32), ("delta", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32), ("ms", ctypes.c_double)]
+                ("bu_div", ctypes.c_uint32), ("ms", ctypes.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ServerConfig(ctypes.Structure):
@@ -115,7 +118,8 @@ class Stats(ctypes.Structure):
                 ("reached_vertices", ctypes.c_uint64), ("reached_edges", ctypes.c_uint64),
                 ("ms_total", ctypes.c_double), ("ms_static", ctypes.c_double), ("ms_ondemand", ctypes.c_double),
                 ("ms_copyout", ctypes.c_double), ("residual", ctypes.c_double),
-                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("kernel_launches", ctypes.c_uint32), ("staged_chunks", ctypes.c_uint32),
+                ("bottom_up_edges", ctypes.c_uint64), ("ms_bottom_up", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "status_detail")}
@@ -236,12 +240,15 @@ def device_free_bytes():
     return free.value
 
 
-def make_budget(frac=None, nbytes=None, edges=None, advise_k=None, fragment_edges=4096, managed=False):
+def make_budget(frac=None, nbytes=None, edges=None, advise_k=None, fragment_edges=4096, managed=False,
+                stage_bytes=0):
     """Static-region budget. managed=True selects the UVM comparison engine
-    (no static region, edges in CUDA managed memory)."""
+    (no static region, edges in CUDA managed memory). stage_bytes of the budget
+    become two staging buffers for dense on-demand passes (standard PageRank)."""
     b = Budget()
     lib().asc_budget_default(ctypes.byref(b))
     b.fragment_edges = fragment_edges
+    b.stage_bytes = int(stage_bytes)
     if managed:
         b.mode, b.value = BUDGET_MANAGED, 0.0
     elif frac is not None:
@@ -397,8 +404,8 @@ def _get_tuning(self):
     return t.as_dict()
 
 
-def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=0):
-    t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, delta, 0, 0.0)
+def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=0, bu_div=16):
+    t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, delta, bu_div, 0.0)
     _check(lib().asc_graph_set_tuning(self._h, ctypes.byref(t)))
 
 

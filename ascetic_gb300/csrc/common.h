@@ -12,6 +12,7 @@
 namespace asc {
 
 struct BatchEngine;
+struct StagePlan;
 
 // Thread-local last-error message (asc_last_error).
 void set_error(const char *fmt, ...);
@@ -41,6 +42,8 @@ struct Tuning {
                                   // holds more than 1/dense_div of the region's vertices; 0 = never
     uint32_t delta = 0;           // SSSP near-far step: distances >= threshold wait in the far set,
                                   // the threshold advances to (min far distance + delta); 0 = off
+    uint32_t bu_div = 16;         // BFS on CSR graphs: a step whose frontier holds more than V / bu_div
+                                  // vertices runs bottom-up over the in-edges; 0 = top-down only
 };
 
 // Per-run device state, sized for one graph and reused across its runs.
@@ -81,6 +84,10 @@ struct Workspace {
     uint32_t *h_list = nullptr;      // page-locked copy of the on-demand frontier list
     uint64_t *h_segs = nullptr;      // page-locked copy of the on-demand segment items
     uint64_t g_cap = 0;              // staging capacity in edges (and in items)
+    StagePlan *stage = nullptr;      // chunk plan of staged PageRank passes, made on first use
+    uint32_t *in_ptr = nullptr;      // in-edge offsets on the device (bottom-up BFS steps)
+    uint32_t *in_edges = nullptr;    // in-edges on the device (only when every out-edge is resident)
+    bool bu_active = false;          // this run's region arguments enable bottom-up steps
 };
 
 }  // namespace asc
@@ -104,6 +111,13 @@ struct asc_graph {
     uint32_t *managed_edges = nullptr;       // ASC_BUDGET_MANAGED: managed copy read instead
     uint32_t *d_ptr = nullptr;
     uint32_t *d_static = nullptr;  // edge prefix [0, static_edges)
+    uint32_t *d_stage[2] = {nullptr, nullptr};  // staging buffers of dense on-demand passes
+    uint64_t stage_words = 0;      // u32 words in each staging buffer (0: no staging)
+    // in-edges of a CSR graph (bottom-up BFS steps), built on first use
+    uint32_t *h_in_ptr = nullptr;  // V+1 offsets (host)
+    uint32_t *h_in_edges = nullptr;  // source ids, a bit stream of in_ebits per edge (pinned, mapped)
+    const uint32_t *d_host_in_edges = nullptr;
+    uint32_t in_ebits = 32;
     uint32_t *d_outdeg = nullptr;
     uint64_t static_edges = 0;
     uint32_t static_vertices = 0;  // S: vertices [0, S) have all edges in the prefix
@@ -151,4 +165,5 @@ asc_status batch_fetch(BatchEngine *b, uint32_t slot, void *out, bool device_out
 uint64_t workspace_bytes(asc_graph *g, bool pagerank);
 // graph.cpp
 asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t param_size);
+asc_status build_in_edges(asc_graph *g);
 }  // namespace asc

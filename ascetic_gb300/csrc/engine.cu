@@ -76,8 +76,9 @@ enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 // Word 28 counts iterations, word 29 flags an iteration cap hit and word 30
 // counts loop-body executions when the loop runs as a CUDA graph. Word 31 is
 // the SSSP near-far threshold, word 36 the minimum far distance of a pass.
+// Words 42-43 (u64): in-edges that bottom-up BFS steps read.
 enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_ITERS = 28, CTL_TIMEOUT = 29, CTL_BODIES = 30, CTL_THRESH = 31,
-       CTL_PR = 32, CTL_MINFAR = 36, CTL_WORDS = 64 };
+       CTL_PR = 32, CTL_MINFAR = 36, CTL_BU_EDGES = 42, CTL_WORDS = 64 };
 
 struct RegionArgs {
     const uint32_t *ptr;
@@ -108,7 +109,21 @@ struct RegionArgs {
     uint32_t wbits;               // > 0: u32 edges packed as (dst << wbits) | weight
     uint32_t ebits;               // bits per stored edge word: 32, or a bit stream of ebits per edge
     unsigned long long *frag;     // non-null: add edges read per 4096-edge fragment
+    // bottom-up BFS steps (null in_ptr: top-down only)
+    const uint32_t *in_ptr;       // in-edge offsets (device)
+    const uint32_t *in_edges;     // in-edge source ids, a bit stream of in_ebits per edge (pinned host)
+    uint32_t in_ebits;
+    uint32_t bu_div;              // a step whose input frontier holds more than V / bu_div vertices is bottom-up
+    uint32_t in_resident;         // in_edges is device memory (a graph without a cap), else pinned host
 };
+
+// True when this BFS iteration steps bottom-up: its input frontier (the
+// region bit counts of the previous step, upper bounds) holds more than
+// V / bu_div vertices. The top-down and bottom-up kernels of an iteration both
+// evaluate it from the same counts and exactly one of them does the work.
+__device__ __forceinline__ bool bottom_up_step(const RegionArgs &a) {
+    return a.in_ptr && a.bu_div && ((uint64_t)a.cnt_in[6] + a.cnt_in[7]) * a.bu_div > a.V;
+}
 
 // Adds the n edges read from [b, b + n) to their 4096-edge fragments' counters.
 __device__ __forceinline__ void count_fragments(unsigned long long *frag, uint64_t b, uint32_t n) {
@@ -433,6 +448,7 @@ __device__ __forceinline__ void flush_next(const RegionArgs &a, uint32_t *s_next
 
 template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_kernel(RegionArgs a) {
+    if (ALG == kBFS && bottom_up_step(a)) return;
     __shared__ Smem sm;
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
@@ -461,6 +477,7 @@ struct FusedArgs {
 
 template <int ALG, int WORDS>
 __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_kernel(FusedArgs x) {
+    if (ALG == kBFS && bottom_up_step(x.r0)) return;
     __shared__ Smem sm;
     __shared__ uint32_t s_next[2];
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
@@ -488,6 +505,80 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
         else expand_item<ALG, WORDS>(x.r0, local, n0, s0, m0, sm, s_next);
     }
     flush_next(x.r0, s_next);
+}
+
+// Bottom-up BFS step (direction-optimizing BFS): every vertex not yet reached
+// scans its in-edges, in source-id order, for a parent in this iteration's
+// frontier and stops at the first one; a vertex found takes the parent's value
+// + 1 (the level-synchronous top-down step gives every unreached vertex with a
+// frontier in-neighbour the same value, so levels are identical) and joins the
+// next frontier. When the frontier is a large part of the graph, most unreached
+// vertices find a parent among their first in-edges, so the step reads far
+// fewer edge bytes over the host link than expanding the frontier's out-lists.
+// One warp per 32-vertex bitmap word, lane = vertex: the warp writes the
+// word's reached and next-frontier bits whole. In-edges are read in place from
+// pinned host memory, kBuUnroll per lane before any frontier probe.
+constexpr int kBuUnroll = 4;
+
+__global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_t nwords) {
+    if (!bottom_up_step(a)) return;
+    __shared__ uint32_t s_next[2];
+    __shared__ unsigned long long s_scanned;
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_scanned = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (kBlock / 32);
+    unsigned long long scanned = 0;
+    for (uint32_t w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); w < nwords; w += warps) {
+        const uint32_t vis = a.visited[w];
+        if (vis == 0xffffffffu) continue;  // the whole warp: every vertex of the word is reached
+        const uint32_t v = 32 * w + lane;
+        uint32_t b = 0, e = 0;
+        if (v < a.V && !((vis >> lane) & 1u)) {
+            b = a.in_ptr[v];
+            e = a.in_ptr[v + 1];
+        }
+        uint32_t nv = 0xffffffffu;
+        for (uint32_t i = b; i < e; i += kBuUnroll) {
+            uint32_t u[kBuUnroll];
+            bool in[kBuUnroll];
+#pragma unroll
+            for (int k = 0; k < kBuUnroll; k++)
+                u[k] = i + k < e ? edge_word(a.in_edges, (uint64_t)i + k, a.in_ebits) : 0xffffffffu;
+#pragma unroll
+            for (int k = 0; k < kBuUnroll; k++)
+                in[k] = u[k] != 0xffffffffu && ((a.bitmap_in[u[k] >> 5] >> (u[k] & 31)) & 1u);
+            int hit = -1;
+#pragma unroll
+            for (int k = kBuUnroll - 1; k >= 0; k--)
+                if (in[k]) hit = k;
+            if (hit >= 0) {
+                nv = a.val[u[hit]] + 1;
+                scanned += (i - b) + (uint32_t)hit + 1;
+                break;
+            }
+        }
+        if (nv == 0xffffffffu) scanned += e - b;
+        const bool won = nv != 0xffffffffu;
+        const unsigned found = __ballot_sync(kFull, won);
+        if (won) a.val[v] = nv;
+        if (lane == 0 && found) {
+            a.visited[w] = vis | found;
+            a.bitmap[w] = found;
+        }
+        count_next(a, won, v, s_next);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) scanned += __shfl_down_sync(kFull, scanned, d);
+    if (lane == 0 && scanned) atomicAdd(&s_scanned, scanned);
+    flush_next(a, s_next);
+    // in-edges are read in place from host memory (resident only on a graph
+    // without a cap): the run's on-demand edges and its bottom-up edges
+    if (threadIdx.x == 0 && s_scanned) {
+        atomicAdd(&a.stats[a.in_resident ? 0 : 1], s_scanned);
+        atomicAdd((unsigned long long *)(a.stats + (CTL_BU_EDGES - CTL_STATS) / 2), s_scanned);
+    }
 }
 
 // Gather-and-copy comparison engine: expands on-demand edges that host
@@ -747,15 +838,17 @@ __global__ void reached_kernel(const uint32_t *val, const uint32_t *ptr, uint32_
 //
 // How the sums of contributions accumulate (PrAcc<T>): FP64 contributions add
 // in FP64, where the order of the atomics changes a sum by about 1e-16
-// relative, far below the stop tolerance. FP32 contributions add exactly, as
-// 64-bit fixed point with 62 fraction bits. Integer addition is associative,
-// so a vertex's sum does not depend on how its edges are split over lanes,
-// warps, tiles, segments or atomics: every pass recomputes bit-identical sums
-// from identical contributions, and the FP64 L1 residual falls to the stop
+// relative, far below the stop tolerance. FP32 contributions add in FP32 only
+// in a fixed order (a thread's own edges, then a warp's segmented shuffle
+// tree), and every partial that meets others through an atomic (across warps,
+// tiles, segments or a scatter's edges) adds exactly, as 64-bit fixed point
+// with 62 fraction bits. Integer addition is associative, so the atomics'
+// order cannot change a sum: every pass recomputes bit-identical sums from
+// identical contributions, and the FP64 L1 residual falls to the stop
 // tolerance. (FP32 atomics in any order floor it near 1.5e-8 at RMAT scale
 // 25, so that such a run always took the pass cap.) A sum is at most the total
-// rank (1 in standard mode), so two integer bits are enough; a contribution
-// below 2^-62 rounds to the grid (an absolute error below 1.1e-19 per edge).
+// rank (1 in standard mode), so two integer bits are enough; a partial below
+// 2^-62 rounds to the grid (an absolute error below 1.1e-19 each).
 template <typename T>
 struct PrAcc;
 template <>
@@ -881,7 +974,7 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
     const int lane = threadIdx.x & 31;
     for (uint32_t base = 0; base < total; base += kBlock) {
         const uint32_t e = base + threadIdx.x;
-        Acc x = (Acc)0;
+        T x = (T)0;
         int owner = -1 - lane;  // distinct per invalid lane
         if (e < total) {
             int lo = 0, hi = kBlock;
@@ -892,17 +985,19 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
             }
             owner = lo;
             const uint32_t srcv = edge_word(a.edges, (uint64_t)sm.start[lo] + (e - sm.pref[lo]), a.ebits);
-            x = PrAcc<T>::from(p.c_old[srcv]);
+            x = p.c_old[srcv];
         }
-        // segmented suffix sum over lanes with the same owner (owners ascend with the lane)
+        // segmented suffix sum over lanes with the same owner (owners ascend
+        // with the lane; a fixed shuffle tree, so the same edges give the same
+        // partial every pass)
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            Acc y = __shfl_down_sync(kFull, x, d);
+            T y = __shfl_down_sync(kFull, x, d);
             int oy = __shfl_down_sync(kFull, owner, d);
             if (lane + d < 32 && oy == owner) x += y;
         }
         int oprev = __shfl_up_sync(kFull, owner, 1);
-        if (owner >= 0 && (lane == 0 || oprev != owner)) atomicAdd(&sm.sum[owner], x);
+        if (owner >= 0 && (lane == 0 || oprev != owner)) atomicAdd(&sm.sum[owner], PrAcc<T>::from(x));
     }
     __syncthreads();
     double res = 0, dang = 0;
@@ -954,12 +1049,12 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
     const uint64_t b = (uint64_t)b0 + (uint64_t)k * a.seg_len;
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
-    Acc x = (Acc)0;
-    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += PrAcc<T>::from(p.c_old[edge_word(a.edges, b + j, a.ebits)]);
+    T x = (T)0;  // this thread's edges in order, then a fixed warp tree
+    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += p.c_old[edge_word(a.edges, b + j, a.ebits)];
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(kFull, x, d);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) sm.sum[w] = x;
+    if (lane == 0) sm.sum[w] = PrAcc<T>::from(x);
     __syncthreads();
     if (threadIdx.x == 0) {
         Acc s = (Acc)0;
@@ -1248,6 +1343,13 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.wbits = g->wbits;
     a.ebits = g->edge_words == 1 ? g->ebits : 32;
     a.frag = ws->frag_active;
+    if (ws->bu_active && ws->in_ptr) {
+        a.in_ptr = ws->in_ptr;
+        a.in_edges = ws->in_edges ? ws->in_edges : g->d_host_in_edges;
+        a.in_resident = ws->in_edges != nullptr;
+        a.in_ebits = g->in_ebits;
+        a.bu_div = ws->tune.bu_div;
+    }
     a.S = g->static_vertices;
     a.V = (uint32_t)g->V;
     a.huge = ws->tune.huge_degree;
@@ -1438,6 +1540,8 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
                     x.work = x.r0.cnt_out + 4;
                     if (near_far(g, algo)) cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, cs);
                     fused(cs, x, grid);
+                    if (algo == ASC_BFS && x.r0.in_ptr)
+                        bottom_up_kernel<<<fill_grid(ws, 32ull * (V / 32 + 1)), kBlock, 0, cs>>>(x.r0, V / 32 + 1);
                     if (near_far(g, algo)) launch_far(g, cs, x.r0);
                     build_frontier_kernel<<<fill_grid(ws, V / 32 + 1), kBlock, 0, cs>>>(x.r0, ws->bitmap[po],
                                                                                         V / 32 + 1);
@@ -1463,6 +1567,264 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
 
 }  // namespace
 
+// ------------------------------------------- staged dense on-demand passes --
+//
+// Standard PageRank reads every edge each pass. On a graph opened with staging
+// buffers (asc_budget.stage_bytes, part of the device budget), the on-demand
+// region is copied each pass in chunks by the copy engine, on a stream of its
+// own, into the two device buffers (chunk k into buffer k % 2), while the
+// kernels consume the chunk before it; the copy of chunk k + 2 waits only for
+// the launch that read chunk k. Chunks end at vertex boundaries, except inside
+// a long list (more than huge_degree edges, summed by segments), which is cut
+// at segment boundaries; a chunk's tile range holds the vertices that start in
+// it, so every vertex is summed exactly once. The static region is cut into as
+// many slices by edges, and launch k runs static slice k with chunk k in one
+// grid (items interleaved), so every launch mixes HBM-bound gathers with the
+// staged chunk and the copies never wait for the static work. The reference
+// moves its gathered partitions into its staging area one at a time with
+// synchronous copies before each partition kernel (CalculateOpt.cu:161-178).
+struct StagePiece {
+    uint32_t v_lo = 0, v_hi = 0;  // tile range: the vertices that start in this piece
+    uint64_t e_lo = 0, e_hi = 0;  // its edges [e_lo, e_hi)
+    std::vector<uint64_t> segs;   // segment items (v << 32 | k) of long lists, in order
+};
+
+struct StageLaunch {
+    uint32_t s_lo = 0, s_hi = 0;  // static slice tile range
+    uint32_t c_lo = 0, c_hi = 0;  // chunk tile range
+    uint64_t w_lo = 0, w_n = 0;   // u32 words the chunk's copy moves (0: no chunk)
+    uint64_t seg_s = 0, seg_c = 0;  // offsets of the slice's and the chunk's segment items
+    uint32_t nseg_s = 0, nseg_c = 0;
+    // work items of the launch: segments plus tiles of kBlock vertices
+    uint64_t items() const {
+        return (uint64_t)nseg_s + nseg_c + (s_hi - s_lo + kBlock - 1) / kBlock + (c_hi - c_lo + kBlock - 1) / kBlock;
+    }
+};
+
+struct StagePlan {
+    uint32_t huge = 0, seg_len = 0;  // the tuning the plan was made for
+    uint32_t chunks = 0;             // launches [0, chunks) carry a chunk
+    std::vector<StageLaunch> launches;
+    uint64_t copy_bytes = 0;         // moved per pass
+    uint64_t *d_segs = nullptr;      // every launch's segment items
+    uint32_t *d_cnt = nullptr;       // per launch, 8 words: [2] slice segments, [3] chunk segments
+    uint32_t *d_work = nullptr;      // per launch work cursor
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+};
+
+void destroy_stage_plan(StagePlan *sp) {
+    if (!sp) return;
+    if (sp->copy) cudaStreamSynchronize(sp->copy);
+    for (void *q : {(void *)sp->d_segs, (void *)sp->d_cnt, (void *)sp->d_work})
+        if (q) cudaFree(q);
+    for (int i = 0; i < 2; i++) {
+        if (sp->copied[i]) cudaEventDestroy(sp->copied[i]);
+        if (sp->consumed[i]) cudaEventDestroy(sp->consumed[i]);
+    }
+    if (sp->copy) cudaStreamDestroy(sp->copy);
+    delete sp;
+}
+
+// u32 words of the stored edge array that hold edges [e_lo, e_hi).
+void edge_words_of(const asc_graph *g, uint64_t e_lo, uint64_t e_hi, uint64_t &w_lo, uint64_t &w_n) {
+    w_lo = w_n = 0;
+    if (e_hi <= e_lo) return;
+    if (g->edge_words == 2) {
+        w_lo = 2 * e_lo;
+        w_n = 2 * (e_hi - e_lo);
+    } else if (g->ebits == 32) {
+        w_lo = e_lo;
+        w_n = e_hi - e_lo;
+    } else {
+        w_lo = (e_lo * g->ebits) >> 5;
+        w_n = ((e_hi * g->ebits - 1) >> 5) - w_lo + 1;
+    }
+}
+
+// Cuts vertices [v0, v1) into pieces whose edges satisfy fits(e_lo, e_hi).
+// False when a single short list or segment does not fit by itself.
+template <typename Fits>
+bool plan_pieces(const uint32_t *ptr, uint32_t v0, uint32_t v1, uint32_t huge, uint32_t seg_len, Fits fits,
+                 std::vector<StagePiece> &out) {
+    StagePiece cur;
+    cur.v_lo = v0;
+    cur.e_lo = cur.e_hi = ptr[v0];
+    auto close = [&](uint32_t v_hi, uint64_t next_e) {
+        cur.v_hi = v_hi;
+        out.push_back(std::move(cur));
+        cur = StagePiece();
+        cur.v_lo = v_hi;
+        cur.e_lo = cur.e_hi = next_e;
+    };
+    for (uint32_t v = v0; v < v1; v++) {
+        const uint64_t b = ptr[v], e = ptr[v + 1];
+        if (e - b <= huge) {
+            if (!fits(cur.e_lo, e)) {
+                if (cur.e_hi == cur.e_lo) return false;
+                close(v, b);
+                if (!fits(cur.e_lo, e)) return false;
+            }
+            cur.e_hi = e;
+            continue;
+        }
+        const uint64_t nseg = (e - b + seg_len - 1) / seg_len;
+        for (uint64_t k = 0; k < nseg; k++) {
+            const uint64_t sb = b + k * seg_len, se = std::min<uint64_t>(e, sb + seg_len);
+            if (!fits(cur.e_lo, se)) {
+                if (cur.e_hi == cur.e_lo) return false;
+                // v belongs to the piece holding its first segment
+                close(k == 0 ? v : v + 1, sb);
+                if (!fits(cur.e_lo, se)) return false;
+            }
+            cur.segs.push_back(((uint64_t)v << 32) | k);
+            cur.e_hi = se;
+        }
+    }
+    cur.v_hi = v1;
+    out.push_back(std::move(cur));
+    return true;
+}
+
+// The chunk plan for the graph's current tuning; *ok false (and no plan) when
+// a long-list segment or a short list does not fit a staging buffer.
+asc_status ensure_stage_plan(asc_graph *g, bool *ok) {
+    Workspace *ws = g->ws;
+    *ok = false;
+    if (!g->stage_words || g->static_edges >= g->E) return ASC_OK;
+    const uint32_t huge = ws->tune.huge_degree, seg_len = ws->tune.segment_edges;
+    if (ws->stage && ws->stage->huge == huge && ws->stage->seg_len == seg_len) {
+        *ok = true;
+        return ASC_OK;
+    }
+    destroy_stage_plan(ws->stage);
+    ws->stage = nullptr;
+    const uint32_t V = (uint32_t)g->V, S = g->static_vertices;
+    std::vector<StagePiece> chunks, slices;
+    const uint64_t cap_words = g->stage_words;
+    if (!plan_pieces(g->h_ptr, S, V, huge, seg_len,
+                     [&](uint64_t lo, uint64_t hi) {
+                         uint64_t w0, wn;
+                         edge_words_of(g, lo, hi, w0, wn);
+                         return wn <= cap_words;
+                     },
+                     chunks))
+        return ASC_OK;
+    // every chunk read stays inside its copy: the short lists of its tile range
+    // and its segments lie in its edges, which fit a buffer; the tile ranges
+    // cover [S, V) once
+    for (size_t k = 0; k < chunks.size(); k++) {
+        const StagePiece &c = chunks[k];
+        uint64_t w0, wn;
+        edge_words_of(g, c.e_lo, c.e_hi, w0, wn);
+        bool good = wn <= cap_words && c.v_lo == (k ? chunks[k - 1].v_hi : S) && c.v_hi >= c.v_lo;
+        for (uint32_t v = c.v_lo; good && v < c.v_hi; v++) {
+            const uint64_t b = g->h_ptr[v], e = g->h_ptr[v + 1];
+            if (e - b <= huge) good = b >= c.e_lo && e <= c.e_hi;
+        }
+        for (uint64_t it : c.segs) {
+            const uint32_t v = (uint32_t)(it >> 32), j = (uint32_t)it;
+            const uint64_t b = (uint64_t)g->h_ptr[v] + (uint64_t)j * seg_len;
+            good = good && b >= c.e_lo && std::min<uint64_t>(g->h_ptr[v + 1], b + seg_len) <= c.e_hi;
+        }
+        if (!good) return fail(ASC_ERR_INVALID, "internal: staging chunk %zu does not cover its reads", k);
+    }
+    if (chunks.back().v_hi != V) return fail(ASC_ERR_INVALID, "internal: staging chunks do not cover the region");
+    const uint64_t static_edges = g->h_ptr[S];
+    if (S > 0) {
+        const uint64_t cap = std::max<uint64_t>({(static_edges + chunks.size() - 1) / chunks.size(),
+                                                 (uint64_t)huge + 1, (uint64_t)seg_len});
+        plan_pieces(g->h_ptr, 0, S, huge, seg_len, [&](uint64_t lo, uint64_t hi) { return hi - lo <= cap; },
+                    slices);
+    }
+    StagePlan *sp = new StagePlan();
+    sp->huge = huge;
+    sp->seg_len = seg_len;
+    sp->chunks = (uint32_t)chunks.size();
+    const size_t L = std::max(chunks.size(), slices.size());
+    std::vector<uint64_t> segs;
+    std::vector<uint32_t> cnt(8 * L, 0);
+    sp->launches.resize(L);
+    for (size_t k = 0; k < L; k++) {
+        StageLaunch &x = sp->launches[k];
+        if (k < slices.size()) {
+            x.s_lo = slices[k].v_lo;
+            x.s_hi = slices[k].v_hi;
+            x.seg_s = segs.size();
+            x.nseg_s = (uint32_t)slices[k].segs.size();
+            cnt[8 * k + 2] = x.nseg_s;
+            segs.insert(segs.end(), slices[k].segs.begin(), slices[k].segs.end());
+        }
+        if (k < chunks.size()) {
+            x.c_lo = chunks[k].v_lo;
+            x.c_hi = chunks[k].v_hi;
+            edge_words_of(g, chunks[k].e_lo, chunks[k].e_hi, x.w_lo, x.w_n);
+            sp->copy_bytes += 4 * x.w_n;
+            x.seg_c = segs.size();
+            x.nseg_c = (uint32_t)chunks[k].segs.size();
+            cnt[8 * k + 3] = x.nseg_c;
+            segs.insert(segs.end(), chunks[k].segs.begin(), chunks[k].segs.end());
+        }
+    }
+    asc_status st = ASC_OK;
+    auto cu = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == ASC_OK) st = cuda_fail(e, what, __FILE__, __LINE__);
+    };
+    cu(cudaMalloc(&sp->d_segs, 8 * std::max<size_t>(1, segs.size())), "cudaMalloc(stage segments)");
+    cu(cudaMalloc(&sp->d_cnt, 4 * cnt.size()), "cudaMalloc(stage counts)");
+    cu(cudaMalloc(&sp->d_work, 4 * L), "cudaMalloc(stage cursors)");
+    if (st == ASC_OK && !segs.empty())
+        cu(cudaMemcpy(sp->d_segs, segs.data(), 8 * segs.size(), cudaMemcpyHostToDevice), "cudaMemcpy(segments)");
+    if (st == ASC_OK) cu(cudaMemcpy(sp->d_cnt, cnt.data(), 4 * cnt.size(), cudaMemcpyHostToDevice), "cudaMemcpy");
+    if (st == ASC_OK) cu(cudaStreamCreateWithFlags(&sp->copy, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (int i = 0; i < 2 && st == ASC_OK; i++) {
+        cu(cudaEventCreateWithFlags(&sp->copied[i], cudaEventDisableTiming), "cudaEventCreate");
+        cu(cudaEventCreateWithFlags(&sp->consumed[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (st != ASC_OK) {
+        destroy_stage_plan(sp);
+        return st;
+    }
+    ws->stage = sp;
+    *ok = true;
+    return ASC_OK;
+}
+
+// Launch k's chunk: its copy on the copy stream once the launch that last read
+// the same buffer is done, and the compute stream s waits for it. Returns the
+// device address that the chunk's edge offsets index (the buffer less the
+// chunk's first word), or the static prefix when launch k has no chunk.
+const uint32_t *stage_chunk(asc_graph *g, StagePlan *sp, uint32_t k, cudaStream_t s, asc_status *st) {
+    const StageLaunch &x = sp->launches[k];
+    *st = ASC_OK;
+    if (!x.w_n) return g->d_static;
+    const int b = k & 1;
+    cudaError_t e = cudaStreamWaitEvent(sp->copy, sp->consumed[b], 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->d_stage[b], g->h_edges + x.w_lo, 4 * x.w_n, cudaMemcpyHostToDevice, sp->copy);
+    if (e == cudaSuccess) e = cudaEventRecord(sp->copied[b], sp->copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, sp->copied[b], 0);
+    if (e != cudaSuccess) *st = cuda_fail(e, "staged chunk copy", __FILE__, __LINE__);
+    return (const uint32_t *)((uintptr_t)g->d_stage[b] - 4 * (uintptr_t)x.w_lo);
+}
+
+asc_status stage_release(StagePlan *sp, uint32_t k, cudaStream_t s) {
+    if (sp->launches[k].w_n) ASC_CUDA(cudaEventRecord(sp->consumed[k & 1], s));
+    return ASC_OK;
+}
+
+// Region arguments of launch k: the static slice (region 0) or the chunk
+// (region 1) with its tile range, segment items, counts and cursor.
+void stage_region(const StagePlan *sp, uint32_t k, int region, const uint32_t *edges, RegionArgs &a) {
+    const StageLaunch &x = sp->launches[k];
+    a.dense_begin = region == 0 ? x.s_lo : x.c_lo;
+    a.dense_end = region == 0 ? x.s_hi : x.c_hi;
+    a.seg_in = sp->d_segs + (region == 0 ? x.seg_s : x.seg_c);
+    a.cnt_in = sp->d_cnt + 8 * k;
+    a.work = sp->d_work + k;
+    if (region == 1) a.edges = edges;
+}
+
 void free_ws_buffers(Workspace *ws) {
     for (void *p : {(void *)ws->val, (void *)ws->visited, (void *)ws->huge_bits, (void *)ws->far_bits,
                     (void *)ws->frag_counts,
@@ -1471,7 +1833,7 @@ void free_ws_buffers(Workspace *ws) {
                     (void *)ws->queue[0],
                     (void *)ws->queue[1],
                     (void *)ws->segs[0], (void *)ws->segs[1], (void *)ws->ctl, (void *)ws->huge_list, ws->pr_rank,
-                    ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum})
+                    ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum, (void *)ws->in_ptr, (void *)ws->in_edges})
         if (p) cudaFree(p);
     if (ws->h_ctl) cudaFreeHost(ws->h_ctl);
     for (void *p : {(void *)ws->g_stage, (void *)ws->g_items})
@@ -1483,6 +1845,8 @@ void free_ws_buffers(Workspace *ws) {
     for (auto e : ws->ev)
         if (e) cudaEventDestroy(e);
     for (auto e : ws->phase_events) cudaEventDestroy(e);
+    destroy_stage_plan(ws->stage);
+    ws->stage = nullptr;
 }
 
 void free_workspace(asc_graph *g) {
@@ -1637,6 +2001,30 @@ asc_status ensure_gather_buffers(asc_graph *g) {
     return ASC_OK;
 }
 
+// In-edge offsets on the device for bottom-up BFS steps, built on the
+// graph's first BFS. The in-edges stay in pinned host memory, read in place,
+// unless the graph has no cap (every out-edge resident): then they are
+// resident too.
+asc_status ensure_in_ptr(asc_graph *g) {
+    Workspace *ws = g->ws;
+    if (ws->in_ptr) return ASC_OK;
+    ASC_TRY(build_in_edges(g));
+    ASC_CUDA(cudaMalloc(&ws->in_ptr, 4 * (g->V + 1)));
+    ASC_CUDA(cudaMemcpy(ws->in_ptr, g->h_in_ptr, 4 * (g->V + 1), cudaMemcpyHostToDevice));
+    ws->device_bytes += 4 * (g->V + 1);
+    if (g->static_edges >= g->E) {
+        const uint64_t words = g->in_ebits == 32 ? std::max<uint64_t>(1, g->E) : (g->E * g->in_ebits + 31) / 32 + 1;
+        ASC_CUDA(cudaMalloc(&ws->in_edges, 4 * words));
+        ASC_CUDA(cudaMemcpy(ws->in_edges, g->h_in_edges, 4 * words, cudaMemcpyHostToDevice));
+        ws->device_bytes += 4 * words;
+    }
+    if (ws->loop_exec[0]) {  // the BFS loop was captured without bottom-up steps
+        cudaGraphExecDestroy(ws->loop_exec[0]);
+        ws->loop_exec[0] = nullptr;
+    }
+    return ASC_OK;
+}
+
 asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, const asc_params &p, void *out,
                               asc_stats *st) {
     Workspace *ws = g->ws;
@@ -1645,6 +2033,12 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     const bool all = algo == ASC_CC;
     uint32_t launches = 0;
     PhaseTimer pt(ws, (p.flags & ASC_RUN_PHASE_TIMING) != 0);
+    // bottom-up steps: BFS on a CSR graph, in the CUDA-graph loop or the host
+    // loop (the per-region timing, fragment counting and gather-and-copy runs
+    // measure the top-down expansion alone)
+    ws->bu_active = algo == ASC_BFS && ws->tune.bu_div && !g->is_csc &&
+                    !(p.flags & (ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY));
+    if (ws->bu_active) ASC_TRY(ensure_in_ptr(g));
     ExpandFn expand = pick_expand(algo, edge_layout(g));
     FusedFn fused = pick_fused(algo, edge_layout(g));
 
@@ -1677,7 +2071,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     const bool use_graph =
         !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY));
     int iters = 0;
-    double phase_ms[2] = {0, 0};
+    double phase_ms[3] = {0, 0, 0};  // static top-down, on-demand top-down, bottom-up
     if (use_graph) {
         const uint32_t gcap = (uint32_t)std::min<int64_t>(cap, 0x7fffffff);
         ASC_TRY(build_loop_graph(g, algo, gcap));
@@ -1720,6 +2114,14 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
                 launches++;
             }
             ASC_TRY(gather_ondemand(g, algo, parity, cnt, ws->ev[3], launches));
+        } else if (pt.on && ws->bu_active && ws->in_ptr && ((uint64_t)cnt[6] + cnt[7]) * ws->tune.bu_div > V) {
+            // diagnostic: a bottom-up step, timed on its own
+            RegionArgs a = region_args(g, parity, 0, false);
+            ASC_TRY(pt.begin(2));
+            pt.record(s);
+            bottom_up_kernel<<<fill_grid(ws, 32ull * nwords), kBlock, 0, s>>>(a, nwords);
+            pt.record(s);
+            launches++;
         } else if (pt.on) {
             // diagnostic: one launch per region, each timed on its own
             if (near_far(g, algo)) ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, s));
@@ -1745,6 +2147,10 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
             if (near_far(g, algo)) ASC_CUDA(cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, s));
             fused(s, x, grid_for(ws, items));
             launches++;
+            if (algo == ASC_BFS && x.r0.in_ptr) {
+                bottom_up_kernel<<<fill_grid(ws, 32ull * nwords), kBlock, 0, s>>>(x.r0, nwords);
+                launches++;
+            }
         }
         {
             RegionArgs out_args = region_args(g, parity, 0, false);
@@ -1763,9 +2169,12 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         if (pt.on) ASC_TRY(pt.sum(phase_ms));
         parity = po;
     }
-    // a BFS expands every reached vertex exactly once, so its expansion counts
-    // already are the reached vertices and edges; SSSP re-expands, so count them
-    if (algo == ASC_SSSP) {
+    // a top-down BFS expands every reached vertex exactly once, so its
+    // expansion counts already are the reached vertices and edges; SSSP
+    // re-expands, and bottom-up steps reach vertices without expanding them,
+    // so count them
+    const bool count_reached = algo == ASC_SSSP || (algo == ASC_BFS && ws->bu_active);
+    if (count_reached) {
         reached_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(ws->val, g->d_ptr, V,
                                                            (unsigned long long *)(ws->ctl + CTL_STATS) + 4);
         launches++;
@@ -1780,26 +2189,32 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     ASC_CUDA(cudaEventRecord(ws->ev[2], s));
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 4 * (CTL_BODIES + 1 - CTL_STATS),
                              cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_BU_EDGES, ws->ctl + CTL_BU_EDGES, 8, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
     if (use_graph) {
         iters = (int)ws->h_ctl[CTL_ITERS];
-        // per body: two expansions, two builds (and two near-far pairs), the loop test
-        launches += (near_far(g, algo) ? 9 : 5) * ws->h_ctl[CTL_BODIES] - 1;
+        // per body: two expansions, two builds (and two near-far pairs, or two
+        // bottom-up kernels), the loop test
+        launches += (near_far(g, algo) ? 9 : (algo == ASC_BFS && ws->bu_active ? 7 : 5)) * ws->h_ctl[CTL_BODIES] - 1;
         if (ws->h_ctl[CTL_TIMEOUT]) return fail(ASC_ERR_TIMEOUT, "no fixpoint after %d iterations", iters);
     }
     if (st) {
         memset(st, 0, sizeof(*st));
         const unsigned long long *hs = (const unsigned long long *)(ws->h_ctl + CTL_STATS);
+        const unsigned long long bu_edges = *(const unsigned long long *)(ws->h_ctl + CTL_BU_EDGES);
         st->iterations = iters;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
+        // out-edges in their stored width, in-edges of bottom-up steps in theirs
+        const unsigned long long bu_od = ws->in_edges ? 0 : bu_edges;
+        st->ondemand_bytes = edge_store_bytes(g, hs[1] - bu_od) + (bu_od * g->in_ebits + 7) / 8;
+        st->bottom_up_edges = bu_edges;
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         if (algo == ASC_CC) {
             st->reached_vertices = V;
             st->reached_edges = g->E;
-        } else if (algo == ASC_BFS) {
+        } else if (algo == ASC_BFS && !count_reached) {
             st->reached_vertices = hs[2] + hs[3];
             st->reached_edges = hs[0] + hs[1];
         } else {
@@ -1813,6 +2228,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         st->ms_copyout = ms;
         st->ms_static = phase_ms[0];
         st->ms_ondemand = phase_ms[1];
+        st->ms_bottom_up = phase_ms[2];
         st->kernel_launches = launches;
     }
     return ASC_OK;
@@ -1876,6 +2292,12 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
     uint32_t cnt[CTL_BLOCK];
     memcpy(cnt, ws->h_ctl, sizeof(cnt));
 
+    // standard PageRank on a graph with staging buffers: the on-demand edges are
+    // copied in chunks every pass, overlapped with the kernels
+    bool staged = false;
+    if (!REF && !pt.on && !(p.flags & ASC_RUN_NO_STAGING)) ASC_TRY(ensure_stage_plan(g, &staged));
+    StagePlan *sp = staged ? ws->stage : nullptr;
+
     // REF: the active set alternates parity like a traversal frontier. STD:
     // every vertex every pass (dense ranges), fixed segment list in parity 0.
     int parity = 0;
@@ -1911,7 +2333,22 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
             const uint32_t nvert = REF ? (bitmap_mode ? range : cnt[region]) : range;
             region_items[region] = (uint64_t)cnt[2 + region] + (nvert + kBlock - 1) / kBlock;
         }
-        if (!pt.on) {
+        if (staged) {
+            ASC_CUDA(cudaMemsetAsync(sp->d_work, 0, 4 * sp->launches.size(), s));
+            for (uint32_t k = 0; k < (uint32_t)sp->launches.size(); k++) {
+                asc_status cs;
+                const uint32_t *chunk_edges = stage_chunk(g, sp, k, s, &cs);
+                ASC_TRY(cs);
+                PrArgs<T> p0 = pa, p1 = pa;
+                p0.r = region_args(g, parity, 0, true);
+                p1.r = region_args(g, parity, 1, true);
+                stage_region(sp, k, 0, chunk_edges, p0.r);
+                stage_region(sp, k, 1, chunk_edges, p1.r);
+                pr_pull_fused_kernel<T, REF><<<grid_for(ws, sp->launches[k].items()), kBlock, 0, s>>>(p0, p1);
+                ASC_TRY(stage_release(sp, k, s));
+                launches++;
+            }
+        } else if (!pt.on) {
             // one launch for both regions (the timed split below runs them apart)
             if (region_items[0] + region_items[1]) {
                 PrArgs<T> p0 = pa, p1 = pa;
@@ -1973,7 +2410,8 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         st->iterations = it;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
+        st->ondemand_bytes = staged ? sp->copy_bytes * (uint64_t)it : edge_store_bytes(g, hs[1]);
+        st->staged_chunks = staged ? sp->chunks * (uint32_t)it : 0;
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         st->reached_vertices = V;
@@ -2717,6 +3155,9 @@ uint64_t workspace_bytes(asc_graph *g, bool pagerank) {
     const uint64_t V = g->V;
     uint64_t b = g->ws ? g->ws->device_bytes : 4 * V + 4 * 4 * (V / 32 + 2) + 8 * V + 8 * (g->E / 256 + 1024) + 4096;
     if (pagerank && (!g->ws || !g->ws->pr_rank)) b += 4ull * 8 * V;
+    // in-edge offsets of bottom-up BFS steps, allocated on the first BFS
+    const uint32_t bu = g->ws ? g->ws->tune.bu_div : (g->has_tuning ? g->tuning.bu_div : Tuning().bu_div);
+    if (!g->is_csc && bu && (!g->ws || !g->ws->in_ptr)) b += 4 * (V + 1);
     return b;
 }
 
@@ -3189,6 +3630,9 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
     ASC_CUDA(cudaGetLastError());
     const int max_it = p.max_iterations > 0 ? p.max_iterations : (REF ? 1000000 : 100);
     const uint32_t grid = (uint32_t)(ws->num_sms * ws->tune.ctas_per_sm);
+    bool staged = false;
+    if (!REF && !(p.flags & ASC_RUN_NO_STAGING)) ASC_TRY(ensure_stage_plan(g, &staged));
+    StagePlan *sp = staged ? ws->stage : nullptr;
     int it = 0;
     double residual = 0;
     for (;;) {
@@ -3214,9 +3658,26 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
         pa.damping = REF ? 0.85 : p.damping;
         pa.acc = acc + 2 * cp;
         pa.dangling_prev = acc + 2 * (1 - cp) + 1;
-        pr_scatter_kernel<T, WORDS><<<grid, kBlock, 0, s>>>(pa);
+        if (staged) {
+            ASC_CUDA(cudaMemsetAsync(sp->d_work, 0, 4 * sp->launches.size(), s));
+            for (uint32_t k = 0; k < (uint32_t)sp->launches.size(); k++) {
+                asc_status cs;
+                const uint32_t *chunk_edges = stage_chunk(g, sp, k, s, &cs);
+                ASC_TRY(cs);
+                PushArgs<T> pk = pa;
+                stage_region(sp, k, 0, chunk_edges, pk.r0);
+                stage_region(sp, k, 1, chunk_edges, pk.r1);
+                pk.work = sp->d_work + k;
+                pr_scatter_kernel<T, WORDS><<<grid_for(ws, sp->launches[k].items()), kBlock, 0, s>>>(pk);
+                ASC_TRY(stage_release(sp, k, s));
+                launches++;
+            }
+        } else {
+            pr_scatter_kernel<T, WORDS><<<grid, kBlock, 0, s>>>(pa);
+            launches++;
+        }
         pr_push_apply_kernel<T, REF><<<fill_grid(ws, V), kBlock, 0, s>>>(pa, V);
-        launches += 2;
+        launches++;
         ASC_CUDA(cudaGetLastError());
         ASC_CUDA(cudaMemcpyAsync(ws->h_ctl, REF ? (void *)active_count : (void *)(acc + 2 * cp), REF ? 4 : 16,
                                  cudaMemcpyDeviceToHost, s));
@@ -3243,7 +3704,8 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
         st->iterations = it;
         st->edges_processed = hs[0] + hs[1];
         st->ondemand_edges = hs[1];
-        st->ondemand_bytes = edge_store_bytes(g, hs[1]);
+        st->ondemand_bytes = staged ? sp->copy_bytes * (uint64_t)it : edge_store_bytes(g, hs[1]);
+        st->staged_chunks = staged ? sp->chunks * (uint32_t)it : 0;
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         st->reached_vertices = V;
@@ -3660,17 +4122,19 @@ std::string tune_cache_path() {
 bool tune_cache_lookup(const std::string &key, asc::Tuning *t) {
     FILE *f = fopen(tune_cache_path().c_str(), "r");
     if (!f) return false;
-    char k[256];
-    unsigned h, sg, d, c, dl;
+    char line[512], k[256];
+    unsigned h, sg, d, c, dl, bu;
     double ms;
     bool found = false;
-    while (fscanf(f, "%255s %u %u %u %u %u %lf", k, &h, &sg, &d, &c, &dl, &ms) == 7)
-        if (key == k) {
+    // one entry per line: key and the eight fields; lines of another layout are skipped
+    while (fgets(line, sizeof(line), f))
+        if (sscanf(line, "%255s %u %u %u %u %u %u %lf", k, &h, &sg, &d, &c, &dl, &bu, &ms) == 8 && key == k) {
             t->huge_degree = h;
             t->segment_edges = sg;
             t->dense_div = d;
             t->ctas_per_sm = c;
             t->delta = dl;
+            t->bu_div = bu;
             found = true;
         }
     fclose(f);
@@ -3686,8 +4150,8 @@ void tune_cache_store(const std::string &key, const asc::Tuning &t, double ms) {
     }
     FILE *f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%s %u %u %u %u %u %.4f\n", key.c_str(), t.huge_degree, t.segment_edges, t.dense_div, t.ctas_per_sm,
-            t.delta, ms);
+    fprintf(f, "%s %u %u %u %u %u %u %.4f\n", key.c_str(), t.huge_degree, t.segment_edges, t.dense_div,
+            t.ctas_per_sm, t.delta, t.bu_div, ms);
     fclose(f);
 }
 
@@ -3719,6 +4183,7 @@ asc_status asc_graph_get_tuning(const asc_graph *g, asc_tuning *t) {
     t->dense_div = d.dense_div;
     t->ctas_per_sm = d.ctas_per_sm;
     t->delta = d.delta;
+    t->bu_div = d.bu_div;
     return ASC_OK;
 }
 
@@ -3730,6 +4195,7 @@ asc_status asc_graph_set_tuning(asc_graph *g, const asc_tuning *t) {
     x.dense_div = t->dense_div;
     x.ctas_per_sm = t->ctas_per_sm;
     x.delta = t->delta;
+    x.bu_div = t->bu_div;
     return asc::set_tuning(g, x);
 }
 
@@ -3774,7 +4240,17 @@ asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, 
     const uint32_t seg_c[] = {1024, 2048, 4096, 8192};
     const uint32_t div_c[] = {8, 16, 32, 64, 256, 0};
     const uint32_t delta_c[] = {0, 16, 32, 64, 128, 256};
+    const uint32_t bu_c[] = {4, 8, 16, 32, 64, 0};
     for (int round = 0; round < 2; round++) {
+        if (algo == ASC_BFS && !g->is_csc)
+            for (uint32_t b : bu_c) {
+                Tuning t = cur;
+                t.bu_div = b;
+                if (t.bu_div == cur.bu_div) continue;
+                double ms;
+                ASC_TRY(measure(t, &ms));
+                if (ms < cur_ms) { cur = t; cur_ms = ms; }
+            }
         if (algo == ASC_SSSP)
             for (uint32_t dl : delta_c) {
                 Tuning t = cur;

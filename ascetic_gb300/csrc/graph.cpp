@@ -17,6 +17,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <new>
 #include <atomic>
 #include <thread>
 
@@ -202,6 +203,17 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : eb;  // budget unit
     uint64_t frag = b->fragment_edges ? b->fragment_edges : 4096;
     uint64_t st = E;
+    // staging buffers come out of a byte budget (at most all of it); the static
+    // prefix gets the rest. An EDGES cap is the prefix alone.
+    double stage = (double)b->stage_bytes;
+    auto prefix_of = [&](double budget_bytes) -> uint64_t {
+        if (budget_bytes / eb >= (double)E) {
+            stage = 0;  // every edge fits: nothing to stage
+            return E;
+        }
+        if (stage > budget_bytes) stage = budget_bytes;
+        return (uint64_t)((budget_bytes - stage) / eb);
+    };
     // every capped mode ends in the reference's rule (GraphMeta.cuh:341-353):
     // the cap in edges, at most E and 2^32 - 1, rounded down to whole fragments
     bool round_down = true;
@@ -214,11 +226,12 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget fraction %g is negative", b->value);
             // the fraction of the source edge-array bytes, spent on device-format edges
             if (b->value * fb >= eb) st = E;
+            else if (stage > 0) st = prefix_of(b->value * (double)E * fb);
             else st = (uint64_t)(b->value * (double)E * fb / eb);
             break;
         case ASC_BUDGET_BYTES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget bytes %g is negative", b->value);
-            st = b->value / eb >= (double)E ? E : (uint64_t)(b->value / eb);
+            st = prefix_of(b->value);
             break;
         case ASC_BUDGET_ADVISE_K: {
             // GraphMeta.cuh:318-354, in 64-bit arithmetic (the reference keeps
@@ -235,6 +248,7 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
                 if (k > 1) k = 1.0;
             }
             st = (uint64_t)((float)k * (double)total_edges);
+            if (stage > 0 && st < E) st = prefix_of((double)st * eb);
             break;
         }
         case ASC_BUDGET_EDGES:
@@ -254,6 +268,11 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
         st -= st % frag;
     }
     g->static_edges = st;
+    // two staging buffers of half the reserve each, 16-byte multiples, when
+    // edges remain on demand; none when the budget leaves less than 8 KiB
+    g->stage_words = 0;
+    if (stage >= 8192 && st < E && b->mode != ASC_BUDGET_ALL && b->mode != ASC_BUDGET_MANAGED)
+        g->stage_words = ((uint64_t)stage / 2) / 16 * 4;
     // S = number of leading vertices whose whole list lies in [0, st); offsets
     // never decrease, so the static vertices are a prefix of the ids.
     uint64_t lo = 0, hi = V;  // find the first v with ptr[v+1] > st
@@ -275,6 +294,7 @@ static asc_status upload(asc_graph *g) {
     uint64_t sb = g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0;
     ASC_CUDA(cudaMalloc(&g->d_static, sb ? sb : 16));
     if (sb) ASC_CUDA(cudaMemcpy(g->d_static, g->h_edges, sb, cudaMemcpyHostToDevice));
+    for (int i = 0; i < 2 && g->stage_words; i++) ASC_CUDA(cudaMalloc(&g->d_stage[i], 4 * g->stage_words));
     if (g->is_csc) {
         ASC_CUDA(cudaMalloc(&g->d_outdeg, sizeof(uint32_t) * g->V));
         ASC_CUDA(cudaMemcpy(g->d_outdeg, g->h_outdeg, sizeof(uint32_t) * g->V, cudaMemcpyHostToDevice));
@@ -376,6 +396,54 @@ static asc_status narrow_edges(asc_graph *g) {
     return ASC_OK;
 }
 
+// n words of src (each < 2^bits) as a bit stream of `bits` per word in new
+// pinned, mapped memory (one padding word at the end).
+static asc_status pack_stream(const uint32_t *src, uint64_t n, uint32_t bits, uint32_t **out) {
+    const uint64_t words = bits == 32 ? (n ? n : 1) : (n * bits + 31) / 32 + 1;
+    uint32_t *packed = nullptr;
+    ASC_TRY(pinned_alloc((void **)&packed, sizeof(uint32_t) * words));
+    if (bits == 32) {
+        parallel_for(n, host_threads(n), [&](unsigned, uint64_t b, uint64_t e) {
+            memcpy(packed + b, src + b, sizeof(uint32_t) * (e - b));
+        });
+        *out = packed;
+        return ASC_OK;
+    }
+    const uint64_t groups = (n + 31) / 32;  // 32 words fill exactly `bits` stream words
+    parallel_for(groups, host_threads(groups * 32), [&](unsigned, uint64_t b, uint64_t e) {
+        for (uint64_t grp = b; grp < e; grp++) {
+            uint32_t *o = packed + grp * bits;
+            for (uint32_t k = 0; k < bits; k++) o[k] = 0;
+            const uint64_t i0 = grp * 32, m = std::min<uint64_t>(32, n - i0);
+            for (uint32_t j = 0; j < m; j++) {
+                const uint32_t v = src[i0 + j], pos = j * bits, w = pos >> 5, sh = pos & 31;
+                o[w] |= v << sh;
+                if (sh + bits > 32) o[w + 1] |= v >> (32 - sh);
+            }
+        }
+    });
+    packed[words - 1] = 0;
+    *out = packed;
+    return ASC_OK;
+}
+
+// Destination of out-edge i in the stored layout.
+static inline uint32_t host_edge_dst(const asc_graph *g, uint64_t i) {
+    if (g->edge_words == 2) return g->h_edges[2 * i];
+    uint32_t w;
+    if (g->ebits == 32) {
+        w = g->h_edges[i];
+    } else {
+        const uint64_t bit = i * g->ebits;
+        const uint32_t *q = g->h_edges + (bit >> 5);
+        const uint32_t sh = (uint32_t)bit & 31u;
+        uint64_t x = q[0] >> sh;
+        if (sh + g->ebits > 32) x |= (uint64_t)q[1] << (32 - sh);
+        w = (uint32_t)x & ((1u << g->ebits) - 1u);
+    }
+    return w >> g->wbits;
+}
+
 static asc_status finish_graph(asc_graph *g, const asc_budget *budget, asc_graph **out) {
     ASC_TRY(validate_and_measure(g));
     g->file_edge_bytes = 4 * g->edge_words;
@@ -393,11 +461,15 @@ static void destroy(asc_graph *g) {
     free_workspace(g);
     if (g->d_ptr) cudaFree(g->d_ptr);
     if (g->d_static) cudaFree(g->d_static);
+    for (uint32_t *p : g->d_stage)
+        if (p) cudaFree(p);
     if (g->d_outdeg) cudaFree(g->d_outdeg);
     if (g->managed_edges) cudaFree(g->managed_edges);
     if (g->h_ptr) cudaFreeHost(g->h_ptr);
     if (g->h_edges) cudaFreeHost(g->h_edges);
     if (g->h_outdeg) cudaFreeHost(g->h_outdeg);
+    if (g->h_in_edges) cudaFreeHost(g->h_in_edges);
+    delete[] g->h_in_ptr;
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -568,6 +640,76 @@ asc_status rmat_build(uint32_t scale, uint32_t ef, uint64_t seed, double a, doub
 }  // namespace
 }  // namespace asc
 
+namespace asc {
+
+// In-edges of a CSR graph for bottom-up BFS steps: a counting sort of the
+// out-edges by destination (host threads), each in-list sorted by source id,
+// stored as a bit stream of bits(V - 1) per edge in pinned memory that the
+// device reads in place. Built once per graph, on its first BFS that may step
+// bottom-up.
+asc_status build_in_edges(asc_graph *g) {
+    if (g->h_in_edges || g->is_csc) return ASC_OK;
+    const uint64_t V = g->V, E = g->E;
+    std::vector<uint32_t> cnt(V + 1, 0);
+    const unsigned nt = host_threads(E);
+    parallel_for(E, nt, [&](unsigned, uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; i++) __atomic_fetch_add(&cnt[host_edge_dst(g, i)], 1u, __ATOMIC_RELAXED);
+    });
+    uint32_t *in_ptr = new (std::nothrow) uint32_t[V + 1];
+    if (!in_ptr) return fail(ASC_ERR_NOMEM, "in-edge offsets: %llu vertices", (unsigned long long)V);
+    uint64_t run = 0;
+    for (uint64_t v = 0; v < V; v++) {
+        in_ptr[v] = (uint32_t)run;
+        run += cnt[v];
+        cnt[v] = in_ptr[v];  // becomes the scatter cursor
+    }
+    in_ptr[V] = (uint32_t)run;
+    std::vector<uint32_t> raw;
+    try {
+        raw.resize(E ? E : 1);
+    } catch (...) {
+        delete[] in_ptr;
+        return fail(ASC_ERR_NOMEM, "in-edges: %llu edges", (unsigned long long)E);
+    }
+    parallel_for(E, nt, [&](unsigned, uint64_t b, uint64_t e) {
+        if (b >= e) return;
+        // the source of edge b: the last vertex whose list starts at or before b
+        uint64_t u = std::upper_bound(g->h_ptr, g->h_ptr + V + 1, (uint32_t)b) - g->h_ptr - 1;
+        for (uint64_t i = b; i < e; i++) {
+            while (g->h_ptr[u + 1] <= i) u++;
+            const uint32_t d = host_edge_dst(g, i);
+            raw[__atomic_fetch_add(&cnt[d], 1u, __ATOMIC_RELAXED)] = (uint32_t)u;
+        }
+    });
+    parallel_for(V, host_threads(E), [&](unsigned, uint64_t b, uint64_t e) {
+        for (uint64_t v = b; v < e; v++) std::sort(raw.begin() + in_ptr[v], raw.begin() + in_ptr[v + 1]);
+    });
+    uint32_t bits = 1;
+    while (bits < 32 && (1ull << bits) < V) bits++;
+    const char *env = getenv("ASC_EDGE_PACKING");
+    if (bits > 30 || (env && env[0] == '0')) bits = 32;
+    uint32_t *packed = nullptr;
+    asc_status st = pack_stream(raw.data(), E, bits, &packed);
+    if (st != ASC_OK) {
+        delete[] in_ptr;
+        return st;
+    }
+    void *dp = nullptr;
+    cudaError_t ce = cudaHostGetDevicePointer(&dp, packed, 0);
+    if (ce != cudaSuccess) {
+        delete[] in_ptr;
+        cudaFreeHost(packed);
+        return cuda_fail(ce, "cudaHostGetDevicePointer(in-edges)", __FILE__, __LINE__);
+    }
+    g->h_in_ptr = in_ptr;
+    g->h_in_edges = packed;
+    g->d_host_in_edges = (const uint32_t *)dp;
+    g->in_ebits = bits;
+    return ASC_OK;
+}
+
+}  // namespace asc
+
 using namespace asc;
 
 extern "C" {
@@ -577,6 +719,7 @@ void asc_budget_default(asc_budget *b) {
     b->mode = ASC_BUDGET_ALL;
     b->fragment_edges = 4096;
     b->value = 0;
+    b->stage_bytes = 0;
 }
 
 asc_status asc_graph_open(const char *path, asc_format fmt, const asc_budget *budget, asc_graph **out) {
@@ -781,7 +924,8 @@ asc_status asc_graph_info_get(const asc_graph *g, asc_graph_info *info) {
     info->is_csc = g->is_csc;
     info->static_edges = g->static_edges;
     info->static_vertices = g->static_vertices;
-    info->device_edge_bytes = g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0;
+    info->staging_bytes = 2 * 4 * g->stage_words;
+    info->device_edge_bytes = (g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0) + info->staging_bytes;
     info->device_vertex_bytes = g->device_vertex_bytes + (g->ws ? g->ws->device_bytes : 0);
     info->host_pinned_bytes = 4ull * edge_store_words(g, g->E);
     info->max_degree = g->max_degree;

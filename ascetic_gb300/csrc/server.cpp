@@ -56,6 +56,10 @@ struct GraphSlot {
     asc::BatchEngine *batch[2] = {nullptr, nullptr};  // BFS, SSSP
     uint64_t batch_bytes[2] = {0, 0};
     uint32_t planes = 0;            // BFS level planes allocated
+    // set while the batch worker uses the engine outside the lock (launch,
+    // collect and the copy-out of finished slots): nobody may free it then,
+    // even when it has just become idle
+    bool in_use[2] = {false, false};
     Query *slot_q[2][64] = {{nullptr}};
     std::deque<Query *> pend[2];    // BFS, SSSP waiting for a slot
 };
@@ -125,7 +129,7 @@ void evict_idle_locked(asc_server *s) {
     for (auto &gs : s->graphs)
         for (int k = 0; k < 2; k++) {
             asc::BatchEngine *b = gs.batch[k];
-            if (!b || asc::batch_busy(b) || !gs.pend[k].empty()) continue;
+            if (!b || gs.in_use[k] || asc::batch_busy(b) || !gs.pend[k].empty()) continue;
             asc::batch_destroy(b);
             gs.batch[k] = nullptr;
             s->used_bytes -= gs.batch_bytes[k];
@@ -270,6 +274,7 @@ void batch_loop(asc_server *s) {
             s->cv_work.wait(lk);
             continue;
         }
+        for (const auto &w : work) s->graphs[w.first].in_use[w.second] = true;
         lk.unlock();
         // one iteration of every busy batch, each on its own stream: all are
         // launched before any is waited for, so their work overlaps on the GPU
@@ -308,6 +313,7 @@ void batch_loop(asc_server *s) {
             }
         }
         lk.lock();
+        for (const auto &w : work) s->graphs[w.first].in_use[w.second] = false;
         for (auto &d : done) finish(s, d.first, d.second);
         s->batches += work.size();
         if (!done.empty()) s->cv_done.notify_all();

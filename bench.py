@@ -23,6 +23,7 @@ python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -37,6 +38,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GTEPS at 25% device budget; served queries/s + p99 latency vs plain engine"
+T_START = time.time()
+
+
+def log(msg):
+    """Progress of the legs on stderr (stdout carries the one JSON line)."""
+    print("[bench %7.1fs] %s" % (time.time() - T_START, msg), file=sys.stderr, flush=True)
 
 
 def parse():
@@ -71,6 +78,10 @@ def parse():
     ap.add_argument("--pr-study", type=int, default=0,
                     help="run only the PageRank precision study on an RMAT graph of this scale (seed 3, "
                          "static region 30%% of edge bytes): FP32 scatter vs FP64 GPU run vs the FP64 oracle")
+    ap.add_argument("--pr-scale", type=int, default=25,
+                    help="RMAT scale of the PageRank leg of the default run (0 skips it)")
+    ap.add_argument("--pr-stage-mib", type=lambda x: [int(v) for v in x.split(",") if v], default=[16, 32, 64, 128],
+                    help="staging sizes (MiB of the budget, two buffers) of the PageRank study's staged passes")
     ap.add_argument("--batch-sssp", action="store_true", help="add a 64-source batched SSSP leg")
     ap.add_argument("--budget-study", action="store_true",
                     help="BFS GTEPS by static fraction of edge bytes (all in HBM down to all on demand)")
@@ -232,10 +243,74 @@ def pr_study(args):
                                     "ondemand_gb_per_pass": round(st["ondemand_bytes"] / st["iterations"] / 1e9, 4),
                                     "ondemand_gbps": round(st["ondemand_bytes"] / (st["ms_total"] * 1e-3) / 1e9, 1)}
     out["fp32_pass_by_budget"] = by_budget
+    # staged passes: part of the same 30% budget held as two staging buffers,
+    # the on-demand edges copied in chunks every pass (copy engine) while the
+    # kernels read the chunk before
+    staged = {}
+    for mib in args.pr_stage_mib:
+        b = A.make_budget(frac=0.30, stage_bytes=mib << 20)
+        with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=b) as g:
+            prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
+            g.run("pr", params=prm)
+            r, st = g.run("pr", params=prm)
+            staged[str(mib)] = {"ms": round(st["ms_total"], 2), "passes": st["iterations"],
+                                "ms_per_pass": round(st["ms_total"] / st["iterations"], 3),
+                                "static_edge_share": round(g.info.static_edges / g.E, 4),
+                                "chunks_per_pass": st["staged_chunks"] // max(1, st["iterations"]),
+                                "copied_gb_per_pass": round(st["ondemand_bytes"] / st["iterations"] / 1e9, 4),
+                                "copy_gbps": round(st["ondemand_bytes"] / (st["ms_total"] * 1e-3) / 1e9, 1),
+                                "max_abs_err_vs_fp64_oracle": float(np.abs(r.astype(np.float64) - exact).max())}
+    out["fp32_staged_by_stage_mib"] = staged
     out["fp32_vs_fp64_gpu_max_abs"] = float(np.abs(res["fp32"][0] - res["fp64"][0]).max())
     out["oracle"] = {"passes": it, "residual": resid, "seconds": round(oracle_s, 1), "threads": oracle_threads()}
     out["within_1e-6"] = bool(out["fp32"]["max_abs_err_vs_fp64_oracle"] <= 1e-6)
     print(json.dumps(out), flush=True)
+
+
+def pagerank_leg(args):
+    """The PageRank precision configuration in every default run: RMAT scale
+    25 (seed 3), in-edge (CSC) arrays, static region 30% of edge bytes,
+    standard PageRank (damping 0.85, stop at FP64 L1 residual < 1e-9 or 100
+    passes); the FP32-contribution run and the all-FP64 run against the FP64
+    host oracle (max-abs, max relative and L1 error per run), and the FP32 run
+    with part of the same budget held as staging buffers for the on-demand
+    edges (copied in chunks each pass) beside the in-place reads."""
+    import ascetic_gb300 as A
+    import oracle
+    sc = args.pr_scale
+    cptr, ccol, od = A.rmat_csr(sc, 16, 3, transpose=True)
+    out = {"rmat_scale": sc, "edges": int(cptr[-1]), "budget_frac": 0.30, "stop": "L1 < 1e-9 or 100 passes"}
+    res = {}
+    with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=0.30)) as g:
+        out["static_edge_share"] = round(g.info.static_edges / g.E, 4)
+        for name, prec in (("fp32", A.F32), ("fp64", A.F64)):
+            prm = A.make_params(pr_mode=A.PR_STD, precision=prec)
+            g.run("pr", params=prm)
+            r, st = g.run("pr", params=prm)
+            res[name] = (r.astype(np.float64), st)
+    stage = args.pr_stage_mib[-1] if args.pr_stage_mib else 128
+    with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=0.30, stage_bytes=stage << 20)) as g:
+        prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
+        g.run("pr", params=prm)
+        r, st = g.run("pr", params=prm)
+        res["fp32_staged"] = (r.astype(np.float64), st)
+        staged_share = round(g.info.static_edges / g.E, 4)
+    t1 = time.perf_counter()
+    exact, it, resid = oracle.pr_std_mt(cptr, ccol, od, oracle_threads())
+    out["oracle"] = {"passes": it, "residual": resid, "seconds": round(time.perf_counter() - t1, 1),
+                     "threads": oracle_threads()}
+    for name, (r, st) in res.items():
+        err = np.abs(r - exact)
+        out[name] = {"ms": round(st["ms_total"], 2), "passes": st["iterations"],
+                     "ms_per_pass": round(st["ms_total"] / st["iterations"], 3), "residual": st["residual"],
+                     "max_abs_err": float(err.max()), "max_rel_err": float((err / exact).max()),
+                     "l1_err": float(err.sum()), "ondemand_gb_per_pass":
+                         round(st["ondemand_bytes"] / st["iterations"] / 1e9, 4)}
+    out["fp32_staged"].update({"stage_mib": stage, "static_edge_share": staged_share,
+                               "chunks_per_pass": res["fp32_staged"][1]["staged_chunks"] //
+                               max(1, res["fp32_staged"][1]["iterations"])})
+    out["within_1e-6"] = all(out[n]["max_abs_err"] <= 1e-6 for n in res)
+    return out
 
 
 def serve_leg(args):
@@ -265,6 +340,7 @@ def serve_leg(args):
         graphs.append(A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=args.budget)))
         del ptr, adj, deg
     t_gen = time.time() - t0
+    log("serving graphs built (%.1f s)" % t_gen)
     std32 = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
     plan = []
     for _ in range(args.serve_queries):
@@ -322,8 +398,11 @@ def serve_leg(args):
     # warm-up (graph loops, batch state) then saturating load
     run(A.SERVE_BATCHED, n=min(40, len(plan)))
     run(A.SERVE_FIFO, n=min(8, len(plan)))
+    log("serving warm-up done")
     sb, kb, wb = run(A.SERVE_BATCHED, keep=True)
+    log("batched server: %d queries in %.1f s" % (len(plan), wb))
     sf, kf, wf = run(A.SERVE_FIFO, n=n_fifo, keep=True)
+    log("plain FIFO engine: %d queries in %.1f s" % (n_fifo, wf))
     exact, pr_err = True, 0.0
     for k in sorted(sample):
         algo = plan[k][1]
@@ -719,6 +798,7 @@ def batch_study(args):
 
 
 def main():
+    faulthandler.enable()
     args = parse()
     if args.pr_study:
         pr_study(args)
@@ -783,6 +863,7 @@ def main():
         od_bytes += st["ondemand_bytes"]
         iters += st["iterations"]
     t_wall = time.perf_counter() - t_wall
+    log("timed BFS steps done: %.1f GTEPS" % (tot_edges / (tot_ms * 1e-3) / 1e9))
     replica_barrier(world)
     clk = clocks.stop()
     job_edges, job_s = replica_reduce(tot_edges, tot_ms * 1e-3, world)
@@ -819,14 +900,19 @@ def main():
            "value_pageable_result": round(pg_edges / pg_s / 1e9, 4),
            "note": "h2d = on-demand edge bytes read over the host link per BFS plus the source id"}
 
-    # phase split and roofline of the expansion kernels
-    ms_s = ms_o = 0.0
-    ed_s = ed_o = vs = vo = 0
+    # phase split and roofline of the kernels: top-down expansion of the
+    # static and of the on-demand region, and the bottom-up steps, each timed
+    # with CUDA events on the engine's stream in phase-timed runs of the same
+    # sources (same levels, same step directions)
+    ms_s = ms_o = ms_b = 0.0
+    ed_s = ed_o = ed_b = vs = vo = 0
     for i in range(8):
         _, st = g.run("bfs", srcs[i], params=A.make_params(flags=A.RUN_NO_OUTPUT | A.RUN_PHASE_TIMING))
         ms_s += st["ms_static"]
         ms_o += st["ms_ondemand"]
-        ed_o += st["ondemand_edges"]
+        ms_b += st["ms_bottom_up"]
+        ed_b += st["bottom_up_edges"]
+        ed_o += st["ondemand_edges"] - st["bottom_up_edges"]
         ed_s += st["edges_processed"] - st["ondemand_edges"]
         vo += st["ondemand_vertices"]
         vs += st["frontier_vertices"] - st["ondemand_vertices"]
@@ -840,26 +926,46 @@ def main():
     link_bytes = eb * ed_o
     dma_gbs, smread_gbs = A.link_probe(1 << 30, 3)
     link_gbs = link_bytes / (ms_o * 1e-3) / 1e9 if ms_o else 0.0
+    # bottom-up: the in-edges it reads cross the host link (a bit stream of
+    # bits(V - 1) per edge, read from the start of each unreached vertex's list
+    # until a frontier parent is found)
+    in_eb = float(np.ceil(np.log2(max(V, 2)))) / 8.0
+    bu_bytes = in_eb * ed_b
+    bu_gbs = bu_bytes / (ms_b * 1e-3) / 1e9 if ms_b else 0.0
+    ms_all = ms_s + ms_o + ms_b
     traffic = load_traffic()
-    dominant = "on-demand" if ms_o >= ms_s else "static"
-    roof_static = {"kernel": "expand_kernel<BFS> static region", "bound": "hbm", "achieved": round(hbm_gbs, 1),
-                   "peak": hbm_peak, "unit": "GB/s", "frac": round(hbm_gbs / hbm_peak, 4),
+    shares = {"static": ms_s, "on-demand": ms_o, "bottom-up": ms_b}
+    dominant = max(shares, key=shares.get)
+    link_common = {"peak_source": "pinned H2D cudaMemcpyAsync measured in this run",
+                   "peak_method": "asc_link_probe: one 1 GiB page-locked buffer copied host to device with "
+                                  "cudaMemcpyAsync, best of 3 (sm_zero_copy_read_peak: the SMs reading the same "
+                                  "buffer in place with 16-byte loads, best of 3)",
+                   "sm_zero_copy_read_peak": round(smread_gbs, 1)}
+    roof_static = {"kernel": "expand_fused_kernel<BFS> static region (top-down)", "bound": "hbm",
+                   "achieved": round(hbm_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                   "frac": round(hbm_gbs / hbm_peak, 4),
                    "traffic": (traffic.get("static") or {}).get("dram_bytes_per_launch"),
                    "traffic_source": "profiles/traffic.json (ncu, DRAM read+write bytes per launch)",
                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
-                   "ms_share": round(ms_s / (ms_s + ms_o), 3) if ms_s + ms_o else None}
-    roof_link = {"kernel": "expand_kernel<BFS> on-demand region", "bound": "host-link",
-                 "achieved": round(link_gbs, 1), "peak": round(dma_gbs, 1), "unit": "GB/s",
-                 "frac": round(link_gbs / dma_gbs, 4) if dma_gbs else None,
-                 "traffic": (traffic.get("ondemand") or {}).get("dram_bytes_per_launch"),
-                 "link_traffic": (traffic.get("ondemand") or {}).get("link_bytes_per_launch"),
-                 "traffic_source": "profiles/traffic.json (ncu: DRAM read+write and host-link sector bytes per "
-                                   "on-demand launch)",
-                 "peak_source": "pinned H2D cudaMemcpyAsync measured in this run",
-                 "sm_zero_copy_read_peak": round(smread_gbs, 1),
-                 "ms_share": round(ms_o / (ms_s + ms_o), 3) if ms_s + ms_o else None}
-    roofline = roof_link if dominant == "on-demand" else roof_static
-    roofline = dict(roofline)
+                   "ms_share": round(ms_s / ms_all, 3) if ms_all else None}
+    roof_link = dict({"kernel": "expand_fused_kernel<BFS> on-demand region (top-down)", "bound": "host-link",
+                      "achieved": round(link_gbs, 1), "peak": round(dma_gbs, 1), "unit": "GB/s",
+                      "frac": round(link_gbs / dma_gbs, 4) if dma_gbs else None,
+                      "traffic": (traffic.get("ondemand") or {}).get("dram_bytes_per_launch"),
+                      "link_traffic": (traffic.get("ondemand") or {}).get("link_bytes_per_launch"),
+                      "traffic_source": "profiles/traffic.json (ncu: DRAM read+write and host-link sector bytes "
+                                        "per on-demand launch)",
+                      "ms_share": round(ms_o / ms_all, 3) if ms_all else None}, **link_common)
+    roof_bu = dict({"kernel": "bottom_up_kernel (BFS bottom-up steps)", "bound": "host-link",
+                    "achieved": round(bu_gbs, 1), "peak": round(dma_gbs, 1), "unit": "GB/s",
+                    "frac": round(bu_gbs / dma_gbs, 4) if dma_gbs else None,
+                    "traffic": (traffic.get("bottom_up") or {}).get("dram_bytes_per_launch"),
+                    "link_traffic": (traffic.get("bottom_up") or {}).get("link_bytes_per_launch"),
+                    "traffic_source": "profiles/traffic.json (ncu, per bottom-up launch)",
+                    "algorithmic_bytes": "in-edges read x bits(V-1)/8",
+                    "in_edges_read_per_bfs": int(ed_b / 8),
+                    "ms_share": round(ms_b / ms_all, 3) if ms_all else None}, **link_common)
+    roofline = dict({"static": roof_static, "on-demand": roof_link, "bottom-up": roof_bu}[dominant])
     roofline["dominant"] = dominant
 
     # parity of the timed workload: the levels of every timed source (run again
@@ -870,14 +976,16 @@ def main():
     ok, o_s = check_rows(0, ptr, col, srcs, lv)
     del lv
     parity["bfs"] = {"sources": len(srcs), "bit_exact": ok, "oracle_s": round(o_s, 1)}
+    log("roofline legs and BFS parity done")
 
     line = {"metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(tot_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic RMAT (seeded)",
             "config": dict(workload_config(args), tuning=tuning and {k: tuning[k] for k in (
-                "huge_degree", "segment_edges", "dense_div", "ctas_per_sm")}, tuning_s=round(t_tune, 2)),
+                "huge_degree", "segment_edges", "dense_div", "ctas_per_sm", "bu_div")}, tuning_s=round(t_tune, 2)),
             "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "roofline": roofline, "roofline_static_hbm": roof_static, "roofline_ondemand_link": roof_link,
+            "roofline_bottom_up_link": roof_bu,
             "graph": {"V": V, "E": int(g.E), "edge_bits": int(info.edge_bits), "static_edges": int(info.static_edges),
                       "static_vertices": int(info.static_vertices), "device_edge_bytes": int(info.device_edge_bytes),
                       "ondemand_bytes_per_bfs": int(od_bytes / args.steps), "iterations_per_bfs": iters / args.steps,
@@ -885,6 +993,7 @@ def main():
             "host_wall_ms_per_step": round(1e3 * t_wall / args.steps, 3)}
     if args.batch:
         line["batch_bfs"] = batch_bfs_leg(A, g, ptr, col, args)
+        log("batch BFS leg done")
         parity["batch_bfs_rows"] = {"rows": line["batch_bfs"]["rows_checked_vs_oracle"],
                                     "bit_exact": line["batch_bfs"]["bit_exact"]}
     g.close()
@@ -892,6 +1001,7 @@ def main():
         line["batch_sssp"] = batch_sssp_leg(A, ptr, budget, args)
 
     if not args.quick:
+        log("SSSP and CC legs")
         extra = {}
         _, adj = A.rmat_csr(args.scale, args.edge_factor, args.seed, weights=(1, 63))
         with A.Graph.from_csr(ptr, adj, budget=budget) as gw:
@@ -931,7 +1041,12 @@ def main():
         line["other_algorithms"] = extra
 
     if args.serve:
+        log("serving leg")
         line["serving"] = serve_leg(args)
+        log("serving leg done")
+    if args.pr_scale and not args.quick:
+        line["pagerank"] = pagerank_leg(args)
+        log("PageRank leg done")
 
     if not args.no_cpu:
         import oracle

@@ -86,6 +86,14 @@ typedef struct asc_budget {
     uint32_t fragment_edges; /* static prefix rounded down to a multiple of this (0 = 4096,
                                 the reference's fragment, GraphMeta.cuh:143,353-354) */
     double value;
+    uint64_t stage_bytes;    /* bytes of the budget held as two staging buffers for dense
+                                on-demand passes (0 = none). The static prefix gets the rest of
+                                a FRAC, BYTES or ADVISE_K budget (an EDGES cap is the prefix
+                                alone). Standard PageRank then copies the on-demand edges each
+                                pass in chunks on a copy stream into the two buffers, overlapped
+                                with the kernels that consume them, as the reference copies its
+                                partitions into its staging area (CalculateOpt.cu:161-178,
+                                GraphMeta.cuh:366-371). Ignored when every edge is static. */
 } asc_budget;
 
 typedef struct asc_graph asc_graph;
@@ -112,6 +120,8 @@ typedef struct asc_graph_info {
                                      and in pinned host memory: more static edges per budget byte,
                                      fewer bytes over the host link; ASC_EDGE_PACKING=0 in the
                                      environment keeps 32) */
+    uint64_t staging_bytes;       /* device staging buffers (asc_budget.stage_bytes; included in
+                                     device_edge_bytes) */
 } asc_graph_info;
 
 typedef enum asc_pr_mode {
@@ -133,6 +143,8 @@ enum {
     ASC_RUN_FRAGMENT_COUNTS = 1u << 4, /* BFS/SSSP/CC: add the edges this run reads to per-fragment
                                           counters (4096 edges a fragment; read them with
                                           asc_graph_fragment_counts); implies ASC_RUN_HOST_LOOP */
+    ASC_RUN_NO_STAGING = 1u << 6,      /* standard PageRank on a graph with staging buffers: read the
+                                          on-demand edges in place (zero-copy) instead of staging */
     ASC_RUN_GATHER_COPY = 1u << 5      /* BFS/SSSP/CC comparison engine, the reference's (and Subway's)
                                           transfer scheme: every iteration the on-demand frontier list
                                           goes to the host, host threads gather its edges into a
@@ -168,7 +180,10 @@ typedef struct asc_stats {
     double ms_copyout;           /* result copy to the caller's buffer */
     double residual;             /* PR std: last FP64 L1 residual */
     uint32_t kernel_launches;    /* kernels of this library launched by the run */
-    uint32_t reserved;
+    uint32_t staged_chunks;      /* chunk copies into the staging buffers (staged PageRank passes);
+                                    ondemand_bytes then counts the bytes those copies moved */
+    uint64_t bottom_up_edges;    /* BFS: in-edges read by bottom-up steps (counted in ondemand_edges) */
+    double ms_bottom_up;         /* with ASC_RUN_PHASE_TIMING: bottom-up BFS kernels */
 } asc_stats;
 
 /* ---- status and errors -------------------------------------------------- */
@@ -242,7 +257,10 @@ typedef struct asc_tuning {
     uint32_t delta;  /* SSSP near-far step: relaxed distances at or above the threshold wait in a far
                         set; when the near frontier empties the threshold moves to the smallest far
                         distance + delta (0: plain frontier relaxation) */
-    uint32_t reserved;
+    uint32_t bu_div; /* BFS on a CSR graph: an iteration whose frontier holds more than V / bu_div
+                        vertices steps bottom-up, every unreached vertex scanning its in-edges for a
+                        frontier parent (in-edges built once on the host, read in place; the device
+                        holds their V + 1 offsets). Same levels. 0: top-down only. Default 16. */
     double ms;
 } asc_tuning;
 enum { ASC_TUNE_NO_CACHE = 1u << 0 };

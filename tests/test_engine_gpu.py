@@ -539,3 +539,70 @@ def test_gather_copy_engine_matches(frac):
             for s in (0, 321):
                 got, _ = g.run("sssp", s, params=gat)
                 assert np.array_equal(got, oracle.sssp(ptr, arr, s))
+
+
+@pytest.mark.parametrize("frac", [0.25, 0.1, 0.0])
+@pytest.mark.parametrize("layout", ["csc", "csr", "csr_weighted"])
+def test_staged_pagerank_equals_zero_copy(frac, layout):
+    """Standard PageRank on a graph with staging buffers copies the on-demand
+    edges in chunks every pass (two 8 KiB buffers here: 10 to 26 chunks, long
+    lists cut between chunks); the ranks equal the zero-copy run's and the
+    oracle's, and the buffers come out of the byte budget."""
+    ptr, col = A.rmat_csr(13, 16, 71)
+    cptr, ccol, od = A.formats.transpose(ptr, col)
+    exp, it, _ = oracle.pr_std(cptr, ccol, od)
+    if layout == "csc":
+        args = (cptr, ccol)
+        kw = {"outdeg": od}
+    elif layout == "csr":
+        args, kw = (ptr, col), {}
+    else:
+        args, kw = (ptr, A.rmat_csr(13, 16, 71, weights=(1, 63))[1]), {}
+    stage = 16 << 10
+    # a zero budget holds no staging either: every edge is then read in place
+    budget = A.make_budget(frac=frac, stage_bytes=stage) if frac else A.make_budget(nbytes=stage,
+                                                                                   stage_bytes=stage)
+    file_bytes = 8 if layout == "csr_weighted" else 4
+    with A.Graph.from_csr(*args, budget=budget, **kw) as g:
+        info = g.info
+        assert info.staging_bytes == stage and (info.static_edges == 0 or frac)
+        assert info.device_edge_bytes <= max(frac * g.E * file_bytes, stage) + 8
+        for tuning in ({}, {"huge_degree": 32, "segment_edges": 256}):
+            if tuning:
+                g.set_tuning(**tuning)
+            for prec in (A.F32, A.F64):
+                zc, st0 = g.run("pr", params=A.make_params(pr_mode=A.PR_STD, precision=prec,
+                                                            flags=A.RUN_NO_STAGING))
+                got, st = g.run("pr", params=A.make_params(pr_mode=A.PR_STD, precision=prec))
+                assert st0["staged_chunks"] == 0 and st["staged_chunks"] >= 5 * st["iterations"], st
+                assert np.abs(got.astype(np.float64) - exp).max() <= PR_TOL, (prec, tuning)
+                # FP32 partials are summed in FP32 within a warp, so tiles cut
+                # at other vertices round differently (relative 1e-7 level)
+                rel = np.abs(got.astype(np.float64) - zc.astype(np.float64)) / exp
+                assert rel.max() <= (1e-5 if prec == A.F32 else 1e-12), (prec, tuning, rel.max())
+                assert abs(st["iterations"] - st0["iterations"]) <= 1
+                assert st["residual"] < 1e-9
+
+
+@pytest.mark.parametrize("frac", [1.0, 0.25, 0.0])
+@pytest.mark.parametrize("bu_div", [0, 16, 1 << 30])
+def test_bottom_up_bfs_levels_equal_top_down(frac, bu_div):
+    """Direction-optimizing BFS: iterations whose frontier holds more than
+    V / bu_div vertices step bottom-up over the in-edges (1 << 30: every
+    iteration, the first included; 0: never). Levels equal the oracle's under
+    the CUDA-graph loop and the host loop, on plain and weighted graphs."""
+    ptr, col = A.rmat_csr(14, 16, 81)
+    _, adj = A.rmat_csr(14, 16, 81, weights=(1, 63))
+    deg = np.diff(ptr)
+    srcs = [0, int(np.nonzero(deg)[0][-1]), int(np.nonzero(deg == 0)[0][0])]
+    for edges in (col, adj):
+        with A.Graph.from_csr(ptr, edges, budget=A.make_budget(frac=frac)) as g:
+            g.set_tuning(bu_div=bu_div)
+            assert g.get_tuning()["bu_div"] == bu_div
+            for s in srcs:
+                exp = oracle.bfs(ptr, col, s)
+                for flags in (0, A.RUN_HOST_LOOP):
+                    got, st = g.run("bfs", s, params=A.make_params(flags=flags))
+                    assert np.array_equal(got, exp), (frac, bu_div, s, flags)
+                    assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
+                    assert st["reached_vertices"] == int((exp != len(ptr)).sum())

@@ -159,3 +159,31 @@ def test_standard_pagerank_scale16_fp32_and_fp64(frac):
                 assert st["iterations"] == passes
             else:
                 assert st["iterations"] <= passes + 5, (st["iterations"], passes)
+
+
+def test_batched_configuration_scale26_rows_equal_oracle():
+    """The batched multi-source configuration: RMAT scale 26, edge factor 16,
+    seed 4, weights uniform in [1, 63], static region 25% of edge bytes; 64
+    seeded sources with out-degree > 0 as one 64-wide BFS batch and one batched
+    SSSP; four rows of each (first, last, two between) bit-exact against the
+    oracle (the reference frontier scheme on all host threads)."""
+    ptr, adj = A.rmat_csr(26, 16, 4, weights=(1, 63))
+    assert len(ptr) - 1 == 1 << 26 and int(ptr[-1]) == 1 << 30
+    deg = np.diff(ptr)
+    rng = np.random.default_rng(4)
+    srcs = [int(x) for x in rng.choice(np.nonzero(deg > 0)[0], size=64, replace=False)]
+    del deg
+    check = [0, 21, 42, 63]
+    threads = os.cpu_count() or 1
+    with A.Graph.from_csr(ptr, adj, budget=A.make_budget(frac=0.25)) as g:
+        assert 0 < g.info.static_edges < g.E
+        for algo, mode in (("bfs", 0), ("sssp", 1)):
+            rows, st = g.run_batch(algo, srcs)
+            assert st["ondemand_edges"] > 0
+            kept = {i: rows[i].copy() for i in check}
+            del rows
+            col = adj[:, 0].copy() if algo == "bfs" else adj
+            for i in check:
+                exp, _ = oracle.relax_mt(mode, ptr, col, srcs[i], threads)
+                assert np.array_equal(kept[i], exp), (algo, i, srcs[i])
+            del col, kept
