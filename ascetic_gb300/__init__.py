@@ -72,7 +72,7 @@ class GraphInfo(ctypes.Structure):
                 ("device_vertex_bytes", ctypes.c_uint64), ("host_pinned_bytes", ctypes.c_uint64),
                 ("max_degree", ctypes.c_uint32), ("max_weight", ctypes.c_uint32),
                 ("weight_bits", ctypes.c_uint32), ("edge_bits", ctypes.c_uint32),
-                ("staging_bytes", ctypes.c_uint64)]
+                ("staging_bytes", ctypes.c_uint64), ("in_head_bytes", ctypes.c_uint64)]
 
 
 class Tuning(ctypes.Structure):

@@ -118,6 +118,9 @@ struct asc_graph {
     uint32_t *h_in_edges = nullptr;  // source ids, a bit stream of in_ebits per edge (pinned, mapped)
     const uint32_t *d_host_in_edges = nullptr;
     uint32_t in_ebits = 32;
+    uint32_t *d_in_heads = nullptr;  // first in-edge per vertex in HBM (from the byte budget), a bit stream
+    uint64_t in_head_words = 0;
+    bool in_heads_ready = false;
     uint32_t *d_outdeg = nullptr;
     uint64_t static_edges = 0;
     uint32_t static_vertices = 0;  // S: vertices [0, S) have all edges in the prefix

@@ -115,6 +115,7 @@ struct RegionArgs {
     uint32_t in_ebits;
     uint32_t bu_div;              // a step whose input frontier holds more than V / bu_div vertices is bottom-up
     uint32_t in_resident;         // in_edges is device memory (a graph without a cap), else pinned host
+    const uint32_t *in_heads;     // first in-edge of every vertex in HBM (a bit stream of in_ebits), or null
 };
 
 // True when this BFS iteration steps bottom-up: its input frontier (the
@@ -540,26 +541,36 @@ __global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_
             e = a.in_ptr[v + 1];
         }
         uint32_t nv = 0xffffffffu;
-        for (uint32_t i = b; i < e; i += kBuUnroll) {
-            uint32_t u[kBuUnroll];
-            bool in[kBuUnroll];
-#pragma unroll
-            for (int k = 0; k < kBuUnroll; k++)
-                u[k] = i + k < e ? edge_word(a.in_edges, (uint64_t)i + k, a.in_ebits) : 0xffffffffu;
-#pragma unroll
-            for (int k = 0; k < kBuUnroll; k++)
-                in[k] = u[k] != 0xffffffffu && ((a.bitmap_in[u[k] >> 5] >> (u[k] & 31)) & 1u);
-            int hit = -1;
-#pragma unroll
-            for (int k = kBuUnroll - 1; k >= 0; k--)
-                if (in[k]) hit = k;
-            if (hit >= 0) {
-                nv = a.val[u[hit]] + 1;
-                scanned += (i - b) + (uint32_t)hit + 1;
-                break;
-            }
+        // the first in-edge is held in HBM, vertex-indexed (a coalesced read):
+        // most unreached vertices find their parent there
+        uint32_t h = b;
+        if (a.in_heads && b < e) {
+            const uint32_t u = edge_word(a.in_heads, v, a.in_ebits);
+            if ((a.bitmap_in[u >> 5] >> (u & 31)) & 1u) nv = a.val[u] + 1;
+            h = b + 1;
         }
-        if (nv == 0xffffffffu) scanned += e - b;
+        if (nv == 0xffffffffu) {
+            for (uint32_t i = h; i < e; i += kBuUnroll) {
+                uint32_t u[kBuUnroll];
+                bool in[kBuUnroll];
+#pragma unroll
+                for (int k = 0; k < kBuUnroll; k++)
+                    u[k] = i + k < e ? edge_word(a.in_edges, (uint64_t)i + k, a.in_ebits) : 0xffffffffu;
+#pragma unroll
+                for (int k = 0; k < kBuUnroll; k++)
+                    in[k] = u[k] != 0xffffffffu && ((a.bitmap_in[u[k] >> 5] >> (u[k] & 31)) & 1u);
+                int hit = -1;
+#pragma unroll
+                for (int k = kBuUnroll - 1; k >= 0; k--)
+                    if (in[k]) hit = k;
+                if (hit >= 0) {
+                    nv = a.val[u[hit]] + 1;
+                    scanned += (i - h) + (uint32_t)hit + 1;
+                    break;
+                }
+            }
+            if (nv == 0xffffffffu) scanned += e - h;
+        }
         const bool won = nv != 0xffffffffu;
         const unsigned found = __ballot_sync(kFull, won);
         if (won) a.val[v] = nv;
@@ -1347,6 +1358,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
         a.in_ptr = ws->in_ptr;
         a.in_edges = ws->in_edges ? ws->in_edges : g->d_host_in_edges;
         a.in_resident = ws->in_edges != nullptr;
+        a.in_heads = g->in_heads_ready ? g->d_in_heads : nullptr;
         a.in_ebits = g->in_ebits;
         a.bu_div = ws->tune.bu_div;
     }

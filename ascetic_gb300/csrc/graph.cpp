@@ -203,16 +203,30 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     const double fb = g->file_edge_bytes ? (double)g->file_edge_bytes : eb;  // budget unit
     uint64_t frag = b->fragment_edges ? b->fragment_edges : 4096;
     uint64_t st = E;
-    // staging buffers come out of a byte budget (at most all of it); the static
-    // prefix gets the rest. An EDGES cap is the prefix alone.
+    // A CSR graph keeps the first in-edge of every vertex in HBM for bottom-up
+    // BFS steps (a bit stream of bits(V - 1) per vertex), and a budget may hold
+    // staging buffers; both come out of a byte budget, the static prefix gets
+    // the rest. An EDGES cap is the prefix alone. Neither is kept when every
+    // edge fits.
+    uint32_t in_bits = 1;
+    while (in_bits < 32 && (1ull << in_bits) < V) in_bits++;
+    const char *pack_env = getenv("ASC_EDGE_PACKING");
+    if (in_bits > 30 || (pack_env && pack_env[0] == '0')) in_bits = 32;
+    g->in_ebits = in_bits;
+    const uint64_t head_words = g->is_csc || !V ? 0 : (in_bits == 32 ? V : (V * in_bits + 31) / 32 + 1);
+    double heads = 4.0 * (double)head_words;
     double stage = (double)b->stage_bytes;
     auto prefix_of = [&](double budget_bytes) -> uint64_t {
         if (budget_bytes / eb >= (double)E) {
-            stage = 0;  // every edge fits: nothing to stage
+            stage = heads = 0;  // every edge fits
             return E;
         }
-        if (stage > budget_bytes) stage = budget_bytes;
-        return (uint64_t)((budget_bytes - stage) / eb);
+        double rest = budget_bytes;
+        if (stage > rest) stage = rest;  // asked for: the staging buffers first
+        rest -= stage;
+        if (heads > rest) heads = 0;  // a budget too small for the heads keeps none
+        rest -= heads;
+        return (uint64_t)(rest / eb);
     };
     // every capped mode ends in the reference's rule (GraphMeta.cuh:341-353):
     // the cap in edges, at most E and 2^32 - 1, rounded down to whole fragments
@@ -221,13 +235,13 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
         case ASC_BUDGET_ALL:
             st = E;
             round_down = false;
+            stage = heads = 0;
             break;
         case ASC_BUDGET_FRAC:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget fraction %g is negative", b->value);
             // the fraction of the source edge-array bytes, spent on device-format edges
             if (b->value * fb >= eb) st = E;
-            else if (stage > 0) st = prefix_of(b->value * (double)E * fb);
-            else st = (uint64_t)(b->value * (double)E * fb / eb);
+            else st = prefix_of(b->value * (double)E * fb);
             break;
         case ASC_BUDGET_BYTES:
             if (!(b->value >= 0)) return fail(ASC_ERR_INVALID, "budget bytes %g is negative", b->value);
@@ -248,7 +262,7 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
                 if (k > 1) k = 1.0;
             }
             st = (uint64_t)((float)k * (double)total_edges);
-            if (stage > 0 && st < E) st = prefix_of((double)st * eb);
+            if (st < E) st = prefix_of((double)st * eb);
             break;
         }
         case ASC_BUDGET_EDGES:
@@ -258,6 +272,7 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
         case ASC_BUDGET_MANAGED:
             st = 0;
             round_down = false;
+            stage = heads = 0;
             break;
         default:
             return fail(ASC_ERR_INVALID, "unknown budget mode %u", b->mode);
@@ -273,6 +288,7 @@ asc_status compute_static_split(asc_graph *g, const asc_budget *b, uint32_t para
     g->stage_words = 0;
     if (stage >= 8192 && st < E && b->mode != ASC_BUDGET_ALL && b->mode != ASC_BUDGET_MANAGED)
         g->stage_words = ((uint64_t)stage / 2) / 16 * 4;
+    g->in_head_words = heads > 0 && st < E ? head_words : 0;
     // S = number of leading vertices whose whole list lies in [0, st); offsets
     // never decrease, so the static vertices are a prefix of the ids.
     uint64_t lo = 0, hi = V;  // find the first v with ptr[v+1] > st
@@ -295,6 +311,10 @@ static asc_status upload(asc_graph *g) {
     ASC_CUDA(cudaMalloc(&g->d_static, sb ? sb : 16));
     if (sb) ASC_CUDA(cudaMemcpy(g->d_static, g->h_edges, sb, cudaMemcpyHostToDevice));
     for (int i = 0; i < 2 && g->stage_words; i++) ASC_CUDA(cudaMalloc(&g->d_stage[i], 4 * g->stage_words));
+    if (g->in_head_words) {  // filled on the graph's first BFS, with the in-edges
+        ASC_CUDA(cudaMalloc(&g->d_in_heads, 4 * g->in_head_words));
+        g->in_heads_ready = false;
+    }
     if (g->is_csc) {
         ASC_CUDA(cudaMalloc(&g->d_outdeg, sizeof(uint32_t) * g->V));
         ASC_CUDA(cudaMemcpy(g->d_outdeg, g->h_outdeg, sizeof(uint32_t) * g->V, cudaMemcpyHostToDevice));
@@ -463,6 +483,7 @@ static void destroy(asc_graph *g) {
     if (g->d_static) cudaFree(g->d_static);
     for (uint32_t *p : g->d_stage)
         if (p) cudaFree(p);
+    if (g->d_in_heads) cudaFree(g->d_in_heads);
     if (g->d_outdeg) cudaFree(g->d_outdeg);
     if (g->managed_edges) cudaFree(g->managed_edges);
     if (g->h_ptr) cudaFreeHost(g->h_ptr);
@@ -684,10 +705,7 @@ asc_status build_in_edges(asc_graph *g) {
     parallel_for(V, host_threads(E), [&](unsigned, uint64_t b, uint64_t e) {
         for (uint64_t v = b; v < e; v++) std::sort(raw.begin() + in_ptr[v], raw.begin() + in_ptr[v + 1]);
     });
-    uint32_t bits = 1;
-    while (bits < 32 && (1ull << bits) < V) bits++;
-    const char *env = getenv("ASC_EDGE_PACKING");
-    if (bits > 30 || (env && env[0] == '0')) bits = 32;
+    const uint32_t bits = g->in_ebits;  // chosen with the split (bits(V - 1), or 32 without packing)
     uint32_t *packed = nullptr;
     asc_status st = pack_stream(raw.data(), E, bits, &packed);
     if (st != ASC_OK) {
@@ -704,7 +722,20 @@ asc_status build_in_edges(asc_graph *g) {
     g->h_in_ptr = in_ptr;
     g->h_in_edges = packed;
     g->d_host_in_edges = (const uint32_t *)dp;
-    g->in_ebits = bits;
+    if (g->d_in_heads && !g->in_heads_ready) {
+        // first in-edge of every vertex (0 where it has none), vertex-indexed
+        std::vector<uint32_t> first(V ? V : 1, 0);
+        parallel_for(V, host_threads(V), [&](unsigned, uint64_t b, uint64_t e) {
+            for (uint64_t v = b; v < e; v++)
+                if (in_ptr[v + 1] > in_ptr[v]) first[v] = raw[in_ptr[v]];
+        });
+        uint32_t *hp = nullptr;
+        ASC_TRY(pack_stream(first.data(), V, bits, &hp));
+        cudaError_t he = cudaMemcpy(g->d_in_heads, hp, 4 * g->in_head_words, cudaMemcpyHostToDevice);
+        cudaFreeHost(hp);
+        if (he != cudaSuccess) return cuda_fail(he, "cudaMemcpy(in-edge heads)", __FILE__, __LINE__);
+        g->in_heads_ready = true;
+    }
     return ASC_OK;
 }
 
@@ -925,7 +956,9 @@ asc_status asc_graph_info_get(const asc_graph *g, asc_graph_info *info) {
     info->static_edges = g->static_edges;
     info->static_vertices = g->static_vertices;
     info->staging_bytes = 2 * 4 * g->stage_words;
-    info->device_edge_bytes = (g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0) + info->staging_bytes;
+    info->in_head_bytes = 4 * g->in_head_words;
+    info->device_edge_bytes = (g->static_edges ? 4ull * edge_store_words(g, g->static_edges) : 0) +
+                              info->staging_bytes + info->in_head_bytes;
     info->device_vertex_bytes = g->device_vertex_bytes + (g->ws ? g->ws->device_bytes : 0);
     info->host_pinned_bytes = 4ull * edge_store_words(g, g->E);
     info->max_degree = g->max_degree;

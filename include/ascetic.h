@@ -122,6 +122,11 @@ typedef struct asc_graph_info {
                                      environment keeps 32) */
     uint64_t staging_bytes;       /* device staging buffers (asc_budget.stage_bytes; included in
                                      device_edge_bytes) */
+    uint64_t in_head_bytes;       /* CSR graphs with edges on demand: the first in-edge of every vertex,
+                                     bits(V - 1) each, held in HBM for bottom-up BFS steps (most unreached
+                                     vertices find their parent there, so those steps barely touch the
+                                     host link); taken from a FRAC / BYTES / ADVISE_K budget like the
+                                     staging buffers, beside an EDGES cap; included in device_edge_bytes */
 } asc_graph_info;
 
 typedef enum asc_pr_mode {

@@ -108,17 +108,23 @@ def test_static_split_modes_follow_reference_rule(packing, monkeypatch):
     ptr, col = A.rmat_csr(16, 16, 1)
     E = int(ptr[-1])
     ptr64 = ptr.astype(np.uint64)
+    # a byte budget also holds the first in-edge of every vertex (bottom-up
+    # BFS steps) when edges stay on demand; the prefix cap is what remains
     for frac in (0.0, 0.05, 0.25, 0.5, 0.999, 1.0):
         with A.Graph.from_csr(ptr, col, budget=A.make_budget(frac=frac)) as g:
             eb = g.info.edge_bits / 8.0
-            cap = E if frac * 4.0 >= eb else int(frac * float(E) * 4.0 / eb)
+            heads = g.info.in_head_bytes
+            cap = E if frac * 4.0 >= eb else int((frac * float(E) * 4.0 - heads) / eb)
             _check_split_against_reference_rule(g, ptr64, cap)
             assert g.info.static_edges % 4096 == 0
+            assert g.info.device_edge_bytes <= max(frac * E * 4.0, 4.0 * E) or frac < 1
     for nbytes in (0, 4095, 1 << 20, 3_000_001, 10 << 20):
         with A.Graph.from_csr(ptr, col, budget=A.make_budget(nbytes=nbytes)) as g:
             eb = g.info.edge_bits / 8.0
-            cap = E if nbytes / eb >= E else int(nbytes / eb)
+            heads = g.info.in_head_bytes
+            cap = E if nbytes / eb >= E else int((nbytes - heads) / eb)
             _check_split_against_reference_rule(g, ptr64, cap)
+            assert g.info.device_edge_bytes <= max(nbytes, 4.0 * E)
     for edges in (1, 4095, 4096, 123_457, E - 1, E, E + 5):
         with A.Graph.from_csr(ptr, col, budget=A.make_budget(edges=edges)) as g:
             _check_split_against_reference_rule(g, ptr64, min(edges, E))
