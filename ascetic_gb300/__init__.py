@@ -32,7 +32,7 @@ BUDGET_ALL, BUDGET_FRAC, BUDGET_BYTES, BUDGET_ADVISE_K, BUDGET_EDGES, BUDGET_MAN
 PR_REF, PR_STD = 0, 1
 F64, F32 = 0, 1
 RUN_NO_OUTPUT, RUN_DEVICE_OUT, RUN_PHASE_TIMING, RUN_HOST_LOOP, RUN_FRAGMENT_COUNTS, RUN_GATHER_COPY = 1, 2, 4, 8, 16, 32
-RUN_NO_STAGING = 64
+RUN_NO_STAGING, RUN_PARTITION_COPY = 64, 128
 RMAT_WEIGHTS, RMAT_SYMMETRIC, RMAT_TRANSPOSE = 1, 2, 4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "cc": CC, "pr": PR}
 

@@ -13,6 +13,7 @@ namespace asc {
 
 struct BatchEngine;
 struct StagePlan;
+struct PartPlan;
 
 // Thread-local last-error message (asc_last_error).
 void set_error(const char *fmt, ...);
@@ -85,6 +86,7 @@ struct Workspace {
     uint64_t *h_segs = nullptr;      // page-locked copy of the on-demand segment items
     uint64_t g_cap = 0;              // staging capacity in edges (and in items)
     StagePlan *stage = nullptr;      // chunk plan of staged PageRank passes, made on first use
+    PartPlan *part = nullptr;        // partitions of the whole-partition comparison engine
     uint32_t *in_ptr = nullptr;      // in-edge offsets on the device (bottom-up BFS steps)
     uint32_t *in_edges = nullptr;    // in-edges on the device (only when every out-edge is resident)
     bool bu_active = false;          // this run's region arguments enable bottom-up steps

@@ -1802,6 +1802,108 @@ asc_status ensure_stage_plan(asc_graph *g, bool *ok) {
     return ASC_OK;
 }
 
+// Whole-partition comparison engine (ASC_RUN_PARTITION_COPY), the reference's
+// baseline of bfs.cu:6-168 / gpu_kernels.cu:302-519: the on-demand region in
+// partitions of one staging buffer, cut at vertex boundaries only; each
+// iteration copies every partition that holds a frontier vertex, whole, and
+// expands that partition's frontier vertices from the copy.
+struct PartPlan {
+    std::vector<StageLaunch> parts;  // c_lo / c_hi (tile range), w_lo / w_n (copy)
+    uint32_t *d_ranges = nullptr;    // per partition: tile range
+    uint32_t *d_flags = nullptr;     // per partition: holds a frontier vertex this iteration
+    uint32_t *h_flags = nullptr;     // page-locked mirror
+    uint32_t *d_cnt = nullptr;       // per partition, 8 words: an id-order walk of its range, no segments
+    uint32_t *d_work = nullptr;      // per partition work cursor
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+};
+
+void destroy_part_plan(PartPlan *pp) {
+    if (!pp) return;
+    if (pp->copy) cudaStreamSynchronize(pp->copy);
+    for (void *q : {(void *)pp->d_ranges, (void *)pp->d_flags, (void *)pp->d_cnt, (void *)pp->d_work})
+        if (q) cudaFree(q);
+    if (pp->h_flags) cudaFreeHost(pp->h_flags);
+    for (int i = 0; i < 2; i++) {
+        if (pp->copied[i]) cudaEventDestroy(pp->copied[i]);
+        if (pp->consumed[i]) cudaEventDestroy(pp->consumed[i]);
+    }
+    if (pp->copy) cudaStreamDestroy(pp->copy);
+    delete pp;
+}
+
+asc_status ensure_part_plan(asc_graph *g) {
+    Workspace *ws = g->ws;
+    if (ws->part) return ASC_OK;
+    if (!g->stage_words)
+        return fail(ASC_ERR_INVALID, "the partition-copy engine needs staging buffers (asc_budget.stage_bytes)");
+    const uint32_t V = (uint32_t)g->V, S = g->static_vertices;
+    std::vector<StagePiece> parts;
+    const uint64_t cap = g->stage_words;
+    if (!plan_pieces(g->h_ptr, S, V, 0xffffffffu, 1u << 30,
+                     [&](uint64_t lo, uint64_t hi) {
+                         uint64_t w0, wn;
+                         edge_words_of(g, lo, hi, w0, wn);
+                         return wn <= cap;
+                     },
+                     parts))
+        return fail(ASC_ERR_BUDGET, "an adjacency list is longer than a partition (%llu words)",
+                    (unsigned long long)cap);
+    PartPlan *pp = new PartPlan();
+    const size_t n = parts.size();
+    std::vector<uint32_t> ranges(2 * n), cnt(8 * n, 0);
+    pp->parts.resize(n);
+    for (size_t k = 0; k < n; k++) {
+        StageLaunch &x = pp->parts[k];
+        x.c_lo = parts[k].v_lo;
+        x.c_hi = parts[k].v_hi;
+        edge_words_of(g, parts[k].e_lo, parts[k].e_hi, x.w_lo, x.w_n);
+        ranges[2 * k] = x.c_lo;
+        ranges[2 * k + 1] = x.c_hi;
+        cnt[8 * k + 7] = 1;  // with dense_div at its maximum: walk the range in id order
+    }
+    asc_status st = ASC_OK;
+    auto cu = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == ASC_OK) st = cuda_fail(e, what, __FILE__, __LINE__);
+    };
+    cu(cudaMalloc(&pp->d_ranges, 8 * n), "cudaMalloc(partition ranges)");
+    cu(cudaMalloc(&pp->d_flags, 4 * n), "cudaMalloc(partition flags)");
+    cu(cudaMalloc(&pp->d_cnt, 32 * n), "cudaMalloc(partition counts)");
+    cu(cudaMalloc(&pp->d_work, 4 * n), "cudaMalloc(partition cursors)");
+    cu(cudaHostAlloc((void **)&pp->h_flags, 4 * n, cudaHostAllocDefault), "cudaHostAlloc(partition flags)");
+    if (st == ASC_OK) cu(cudaMemcpy(pp->d_ranges, ranges.data(), 8 * n, cudaMemcpyHostToDevice), "cudaMemcpy");
+    if (st == ASC_OK) cu(cudaMemcpy(pp->d_cnt, cnt.data(), 32 * n, cudaMemcpyHostToDevice), "cudaMemcpy");
+    if (st == ASC_OK) cu(cudaStreamCreateWithFlags(&pp->copy, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (int i = 0; i < 2 && st == ASC_OK; i++) {
+        cu(cudaEventCreateWithFlags(&pp->copied[i], cudaEventDisableTiming), "cudaEventCreate");
+        cu(cudaEventCreateWithFlags(&pp->consumed[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (st != ASC_OK) {
+        destroy_part_plan(pp);
+        return st;
+    }
+    ws->part = pp;
+    return ASC_OK;
+}
+
+// One CTA per partition (grid-stride): whether its tile range holds a vertex
+// of this iteration's frontier.
+__global__ void part_active_kernel(const uint32_t *bitmap_in, const uint32_t *ranges, uint32_t n,
+                                   uint32_t *flags) {
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint32_t lo = ranges[2 * k], hi = ranges[2 * k + 1];
+        uint32_t any = 0;
+        for (uint32_t u0 = (lo & ~31u) + 32 * threadIdx.x; u0 < hi; u0 += 32 * blockDim.x) {
+            uint32_t w = bitmap_in[u0 >> 5];
+            if (u0 < lo) w &= 0xffffffffu << (lo - u0);
+            if (hi - u0 < 32u) w &= (1u << (hi - u0)) - 1u;
+            any |= w;
+        }
+        any = __syncthreads_or(any != 0);
+        if (threadIdx.x == 0) flags[k] = any;
+    }
+}
+
 // Launch k's chunk: its copy on the copy stream once the launch that last read
 // the same buffer is done, and the compute stream s waits for it. Returns the
 // device address that the chunk's edge offsets index (the buffer less the
@@ -1859,6 +1961,8 @@ void free_ws_buffers(Workspace *ws) {
     for (auto e : ws->phase_events) cudaEventDestroy(e);
     destroy_stage_plan(ws->stage);
     ws->stage = nullptr;
+    destroy_part_plan(ws->part);
+    ws->part = nullptr;
 }
 
 void free_workspace(asc_graph *g) {
@@ -2049,7 +2153,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     // loop (the per-region timing, fragment counting and gather-and-copy runs
     // measure the top-down expansion alone)
     ws->bu_active = algo == ASC_BFS && ws->tune.bu_div && !g->is_csc &&
-                    !(p.flags & (ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY));
+                    !(p.flags & (ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY | ASC_RUN_PARTITION_COPY));
     if (ws->bu_active) ASC_TRY(ensure_in_ptr(g));
     ExpandFn expand = pick_expand(algo, edge_layout(g));
     FusedFn fused = pick_fused(algo, edge_layout(g));
@@ -2080,8 +2184,12 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     // built without counters
     const bool gather = (p.flags & ASC_RUN_GATHER_COPY) != 0;
     if (gather) ASC_TRY(ensure_gather_buffers(g));
-    const bool use_graph =
-        !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS | ASC_RUN_GATHER_COPY));
+    const bool part = !gather && (p.flags & ASC_RUN_PARTITION_COPY) != 0;
+    if (part) ASC_TRY(ensure_part_plan(g));
+    uint64_t part_bytes = 0;
+    uint32_t part_copies = 0;
+    const bool use_graph = !(p.flags & (ASC_RUN_PHASE_TIMING | ASC_RUN_HOST_LOOP | ASC_RUN_FRAGMENT_COUNTS |
+                                        ASC_RUN_GATHER_COPY | ASC_RUN_PARTITION_COPY));
     int iters = 0;
     double phase_ms[3] = {0, 0, 0};  // static top-down, on-demand top-down, bottom-up
     if (use_graph) {
@@ -2126,6 +2234,51 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
                 launches++;
             }
             ASC_TRY(gather_ondemand(g, algo, parity, cnt, ws->ev[3], launches));
+        } else if (part) {
+            // the static region in place, then every on-demand partition that
+            // holds a frontier vertex: copied whole, its frontier expanded from
+            // the copy (partition j of this run into buffer j % 2)
+            const uint64_t items0 = region_work(0);
+            if (items0) {
+                RegionArgs a = region_args(g, parity, 0, false);
+                attach_far(g, algo, a);
+                expand(g, a, grid_for(ws, items0));
+                launches++;
+            }
+            PartPlan *pp = ws->part;
+            const uint32_t np = (uint32_t)pp->parts.size();
+            if (cnt[7]) {
+                part_active_kernel<<<std::min<uint32_t>(np, ws->num_sms * 8), kBlock, 0, s>>>(
+                    ws->bitmap[parity], pp->d_ranges, np, pp->d_flags);
+                ASC_CUDA(cudaMemsetAsync(pp->d_work, 0, 4ull * np, s));
+                ASC_CUDA(cudaMemcpyAsync(pp->h_flags, pp->d_flags, 4ull * np, cudaMemcpyDeviceToHost, s));
+                ASC_CUDA(cudaStreamSynchronize(s));
+                launches++;
+            }
+            for (uint32_t k = 0; cnt[7] && k < np; k++) {
+                if (!pp->h_flags[k]) continue;
+                const StageLaunch &x = pp->parts[k];
+                const int b = part_copies & 1;
+                ASC_CUDA(cudaStreamWaitEvent(pp->copy, pp->consumed[b], 0));
+                ASC_CUDA(cudaMemcpyAsync(g->d_stage[b], g->h_edges + x.w_lo, 4 * x.w_n, cudaMemcpyHostToDevice,
+                                         pp->copy));
+                ASC_CUDA(cudaEventRecord(pp->copied[b], pp->copy));
+                ASC_CUDA(cudaStreamWaitEvent(s, pp->copied[b], 0));
+                RegionArgs a = region_args(g, parity, 1, false);
+                attach_far(g, algo, a);
+                a.edges = (const uint32_t *)((uintptr_t)g->d_stage[b] - 4 * (uintptr_t)x.w_lo);
+                a.dense_begin = x.c_lo;
+                a.dense_end = x.c_hi;
+                a.cnt_in = pp->d_cnt + 8ull * k;  // id-order walk of the range, no segments
+                a.dense_div = 0xffffffffu;
+                a.huge = 0xffffffffu;             // long lists too are expanded from the copy
+                a.work = pp->d_work + k;
+                expand(g, a, grid_for(ws, (x.c_hi - (x.c_lo & ~31u) + kBlock - 1) / kBlock));
+                ASC_CUDA(cudaEventRecord(pp->consumed[b], s));
+                launches++;
+                part_copies++;
+                part_bytes += 4 * x.w_n;
+            }
         } else if (pt.on && ws->bu_active && ws->in_ptr && ((uint64_t)cnt[6] + cnt[7]) * ws->tune.bu_div > V) {
             // diagnostic: a bottom-up step, timed on its own
             RegionArgs a = region_args(g, parity, 0, false);
@@ -2220,6 +2373,10 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         // out-edges in their stored width, in-edges of bottom-up steps in theirs
         const unsigned long long bu_od = ws->in_edges ? 0 : bu_edges;
         st->ondemand_bytes = edge_store_bytes(g, hs[1] - bu_od) + (bu_od * g->in_ebits + 7) / 8;
+        if (part) {  // what the partition copies moved
+            st->ondemand_bytes = part_bytes;
+            st->staged_chunks = part_copies;
+        }
         st->bottom_up_edges = bu_edges;
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];

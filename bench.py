@@ -598,6 +598,29 @@ def gather_study(args):
     out["zero_copy_speedup"] = round(out["gather_copy"]["ms_per_bfs"] / out["zero_copy"]["ms_per_bfs"], 2)
     out["zero_copy_speedup_32bit"] = round(out["gather_copy_32bit"]["ms_per_bfs"] /
                                            out["zero_copy_32bit"]["ms_per_bfs"], 2)
+    # the reference's whole-partition baseline (bfs.cu:6-168): every partition
+    # holding a frontier vertex copied whole each iteration. As the reference
+    # runs it, the whole budget is the partition buffers (no static region);
+    # beside it, a static prefix with 64 MiB of the budget as the buffers.
+    budget_bytes = args.budget * 4.0 * int(ptr[-1])
+    for name, b in (("partition_copy", A.make_budget(nbytes=budget_bytes, stage_bytes=int(budget_bytes))),
+                    ("partition_copy_with_static",
+                     A.make_budget(frac=args.budget, stage_bytes=64 << 20))):
+        with A.Graph.from_csr(ptr, col, budget=b) as g:
+            prm = A.make_params(flags=A.RUN_NO_OUTPUT | A.RUN_PARTITION_COPY)
+            g.run("bfs", srcs[0], params=prm)
+            ms, edges, moved, copies = 0.0, 0, 0, 0
+            for s_ in srcs:
+                _, st = g.run("bfs", s_, params=prm)
+                ms += st["ms_total"]
+                edges += st["reached_edges"]
+                moved += st["ondemand_bytes"]
+                copies += st["staged_chunks"]
+            out[name] = {"ms_per_bfs": round(ms / len(srcs), 3), "gteps": round(edges / (ms * 1e-3) / 1e9, 2),
+                         "static_edge_share": round(g.info.static_edges / g.E, 4),
+                         "partition_bytes": int(g.info.staging_bytes // 2),
+                         "copied_bytes_per_bfs": int(moved / len(srcs)),
+                         "partition_copies_per_bfs": round(copies / len(srcs), 1)}
     print(json.dumps(out), flush=True)
 
 

@@ -150,13 +150,22 @@ enum {
                                           asc_graph_fragment_counts); implies ASC_RUN_HOST_LOOP */
     ASC_RUN_NO_STAGING = 1u << 6,      /* standard PageRank on a graph with staging buffers: read the
                                           on-demand edges in place (zero-copy) instead of staging */
-    ASC_RUN_GATHER_COPY = 1u << 5      /* BFS/SSSP/CC comparison engine, the reference's (and Subway's)
+    ASC_RUN_GATHER_COPY = 1u << 5,     /* BFS/SSSP/CC comparison engine, the reference's (and Subway's)
                                           transfer scheme: every iteration the on-demand frontier list
                                           goes to the host, host threads gather its edges into a
                                           page-locked staging buffer, one copy moves them to the
                                           device and a kernel expands them there (GraphMeta.cuh:469-578,
                                           CalculateOpt.cu:146-178); the static region runs as usual.
                                           Same values; implies ASC_RUN_HOST_LOOP */
+    ASC_RUN_PARTITION_COPY = 1u << 7   /* BFS/SSSP/CC comparison engine, the reference's whole-partition
+                                          baseline (bfs.cu:6-168, gpu_kernels.cu:302-519): the on-demand
+                                          region is cut into partitions of one staging buffer (vertex
+                                          boundaries; a list longer than a buffer is an error, as in the
+                                          reference), and every iteration each partition holding an
+                                          active vertex is copied whole and its active vertices expanded
+                                          from the copy; the static region runs as usual. Needs a graph
+                                          opened with asc_budget.stage_bytes. Same values; implies
+                                          ASC_RUN_HOST_LOOP */
 };
 
 typedef struct asc_params {

@@ -606,3 +606,41 @@ def test_bottom_up_bfs_levels_equal_top_down(frac, bu_div):
                     assert np.array_equal(got, exp), (frac, bu_div, s, flags)
                     assert st["reached_edges"] == oracle.reached_edges(ptr, exp, len(ptr))
                     assert st["reached_vertices"] == int((exp != len(ptr)).sum())
+
+
+@pytest.mark.parametrize("frac", [0.25, 0.0])
+def test_partition_copy_engine_matches(frac):
+    """The whole-partition comparison engine (the reference's baseline: every
+    partition holding a frontier vertex copied whole each iteration) gives the
+    oracle's values; with a zero budget it is the reference's configuration
+    (every edge in partitions, no static region)."""
+    stage = 64 << 10
+    mk = (lambda: A.make_budget(frac=frac, stage_bytes=stage)) if frac else \
+        (lambda: A.make_budget(nbytes=stage, stage_bytes=stage))
+    prm = A.make_params(flags=A.RUN_PARTITION_COPY)
+    ptr, adj = A.rmat_csr(13, 16, 91, weights=(1, 63))
+    col = adj[:, 0].copy()
+    sptr, scol = A.formats.symmetrize(ptr, col)
+    with A.Graph.from_csr(ptr, col, budget=mk()) as g:
+        assert g.info.staging_bytes == stage and (frac or g.info.static_edges == 0)
+        for s in (0, 1000):
+            got, st = g.run("bfs", s, params=prm)
+            assert np.array_equal(got, oracle.bfs(ptr, col, s)), s
+            assert st["staged_chunks"] > 0 and st["ondemand_bytes"] > 0
+    with A.Graph.from_csr(ptr, adj, budget=mk()) as g:
+        got, _ = g.run("sssp", 5, params=prm)
+        assert np.array_equal(got, oracle.sssp(ptr, adj, 5))
+    with A.Graph.from_csr(sptr, scol, budget=mk()) as g:
+        got, _ = g.run("cc", params=prm)
+        assert np.array_equal(got, oracle.cc(sptr, scol))
+
+
+def test_partition_copy_rejects_a_list_longer_than_a_partition():
+    V = 12000
+    ptr = np.zeros(V + 1, np.uint64)
+    ptr[1:] = V - 1                     # vertex 0 points at every other vertex
+    col = np.arange(1, V, dtype=np.uint32)
+    with A.Graph.from_csr(ptr, col, budget=A.make_budget(nbytes=8 << 10, stage_bytes=8 << 10)) as g:
+        with pytest.raises(A.AscError) as e:
+            g.run("bfs", 0, params=A.make_params(flags=A.RUN_PARTITION_COPY))
+        assert e.value.status == A.ERR_BUDGET
