@@ -404,7 +404,7 @@ def _get_tuning(self):
     return t.as_dict()
 
 
-def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=0, bu_div=16):
+def _set_tuning(self, huge_degree=512, segment_edges=2048, dense_div=64, ctas_per_sm=0, delta=0, bu_div=64):
     t = Tuning(huge_degree, segment_edges, dense_div, ctas_per_sm, delta, bu_div, 0.0)
     _check(lib().asc_graph_set_tuning(self._h, ctypes.byref(t)))
 

@@ -43,7 +43,7 @@ struct Tuning {
                                   // holds more than 1/dense_div of the region's vertices; 0 = never
     uint32_t delta = 0;           // SSSP near-far step: distances >= threshold wait in the far set,
                                   // the threshold advances to (min far distance + delta); 0 = off
-    uint32_t bu_div = 16;         // BFS on CSR graphs: a step whose frontier holds more than V / bu_div
+    uint32_t bu_div = 64;         // BFS on CSR graphs: a step whose frontier holds more than V / bu_div
                                   // vertices runs bottom-up over the in-edges; 0 = top-down only
 };
 

@@ -4409,7 +4409,7 @@ asc_status asc_graph_tune(asc_graph *g, asc_algo algo, const uint32_t *sources, 
     const uint32_t seg_c[] = {1024, 2048, 4096, 8192};
     const uint32_t div_c[] = {8, 16, 32, 64, 256, 0};
     const uint32_t delta_c[] = {0, 16, 32, 64, 128, 256};
-    const uint32_t bu_c[] = {4, 8, 16, 32, 64, 0};
+    const uint32_t bu_c[] = {8, 16, 32, 64, 128, 256, 0};
     for (int round = 0; round < 2; round++) {
         if (algo == ASC_BFS && !g->is_csc)
             for (uint32_t b : bu_c) {

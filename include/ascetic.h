@@ -274,7 +274,7 @@ typedef struct asc_tuning {
     uint32_t bu_div; /* BFS on a CSR graph: an iteration whose frontier holds more than V / bu_div
                         vertices steps bottom-up, every unreached vertex scanning its in-edges for a
                         frontier parent (in-edges built once on the host, read in place; the device
-                        holds their V + 1 offsets). Same levels. 0: top-down only. Default 16. */
+                        holds their V + 1 offsets). Same levels. 0: top-down only. Default 64. */
     double ms;
 } asc_tuning;
 enum { ASC_TUNE_NO_CACHE = 1u << 0 };

@@ -151,7 +151,9 @@ def test_packed_and_unpacked_weighted_edges():
             assert g.info.edge_bytes == (4 if packed else 8)
             assert g.info.edge_bits == (19 if packed else 64)
             frac_edges = g.info.static_edges / g.E
-            assert abs(frac_edges - 0.2 * 64 / g.info.edge_bits) < 0.05, frac_edges
+            # the byte budget also holds the first in-edge of every vertex
+            expect = (0.2 * 8 * g.E - g.info.in_head_bytes) / (g.info.edge_bits / 8) / g.E
+            assert abs(frac_edges - expect) < 0.05, (frac_edges, expect)
             for s in (0, 41):
                 got, _ = g.run("sssp", s)
                 assert np.array_equal(got, oracle.sssp(ptr, arr, s)), (packed, s)
