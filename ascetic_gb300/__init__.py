@@ -119,7 +119,8 @@ class Stats(ctypes.Structure):
                 ("ms_total", ctypes.c_double), ("ms_static", ctypes.c_double), ("ms_ondemand", ctypes.c_double),
                 ("ms_copyout", ctypes.c_double), ("residual", ctypes.c_double),
                 ("kernel_launches", ctypes.c_uint32), ("staged_chunks", ctypes.c_uint32),
-                ("bottom_up_edges", ctypes.c_uint64), ("ms_bottom_up", ctypes.c_double)]
+                ("bottom_up_edges", ctypes.c_uint64), ("ms_bottom_up", ctypes.c_double),
+                ("bottom_up_vertices", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "status_detail")}

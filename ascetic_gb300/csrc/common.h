@@ -89,6 +89,7 @@ struct Workspace {
     PartPlan *part = nullptr;        // partitions of the whole-partition comparison engine
     uint32_t *in_ptr = nullptr;      // in-edge offsets on the device (bottom-up BFS steps)
     uint32_t *in_edges = nullptr;    // in-edges on the device (only when every out-edge is resident)
+    uint32_t *in_none = nullptr;     // one bit per vertex without in-edges
     bool bu_active = false;          // this run's region arguments enable bottom-up steps
 };
 

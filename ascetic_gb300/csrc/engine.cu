@@ -76,9 +76,10 @@ enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 // Word 28 counts iterations, word 29 flags an iteration cap hit and word 30
 // counts loop-body executions when the loop runs as a CUDA graph. Word 31 is
 // the SSSP near-far threshold, word 36 the minimum far distance of a pass.
-// Words 42-43 (u64): in-edges that bottom-up BFS steps read.
+// Words 42-43 (u64): in-edges that bottom-up BFS steps read from host memory;
+// words 44-45 (u64): unreached vertices those steps examined.
 enum { CTL_BLOCK = 8, CTL_STATS = 16, CTL_ITERS = 28, CTL_TIMEOUT = 29, CTL_BODIES = 30, CTL_THRESH = 31,
-       CTL_PR = 32, CTL_MINFAR = 36, CTL_BU_EDGES = 42, CTL_WORDS = 64 };
+       CTL_PR = 32, CTL_MINFAR = 36, CTL_BU_EDGES = 42, CTL_BU_VERTS = 44, CTL_WORDS = 64 };
 
 struct RegionArgs {
     const uint32_t *ptr;
@@ -116,6 +117,7 @@ struct RegionArgs {
     uint32_t bu_div;              // a step whose input frontier holds more than V / bu_div vertices is bottom-up
     uint32_t in_resident;         // in_edges is device memory (a graph without a cap), else pinned host
     const uint32_t *in_heads;     // first in-edge of every vertex in HBM (a bit stream of in_ebits), or null
+    const uint32_t *in_none;      // one bit per vertex without in-edges (never reached but as a source)
 };
 
 // True when this BFS iteration steps bottom-up: its input frontier (the
@@ -524,32 +526,39 @@ constexpr int kBuUnroll = 4;
 __global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_t nwords) {
     if (!bottom_up_step(a)) return;
     __shared__ uint32_t s_next[2];
-    __shared__ unsigned long long s_scanned;
+    __shared__ unsigned long long s_scanned, s_examined;
     if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
-    if (threadIdx.x == 0) s_scanned = 0;
+    if (threadIdx.x == 0) s_scanned = s_examined = 0;
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (kBlock / 32);
-    unsigned long long scanned = 0;
+    unsigned long long scanned = 0, examined = 0;
     for (uint32_t w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); w < nwords; w += warps) {
         const uint32_t vis = a.visited[w];
-        if (vis == 0xffffffffu) continue;  // the whole warp: every vertex of the word is reached
+        // vertices without in-edges can never be reached: about half of an
+        // RMAT graph, nearly all of its unreachable vertices
+        const uint32_t done = vis | a.in_none[w];
+        if (done == 0xffffffffu) continue;  // the whole warp: nothing to look for in this word
         const uint32_t v = 32 * w + lane;
-        uint32_t b = 0, e = 0;
-        if (v < a.V && !((vis >> lane) & 1u)) {
-            b = a.in_ptr[v];
-            e = a.in_ptr[v + 1];
-        }
-        uint32_t nv = 0xffffffffu;
-        // the first in-edge is held in HBM, vertex-indexed (a coalesced read):
-        // most unreached vertices find their parent there
-        uint32_t h = b;
-        if (a.in_heads && b < e) {
+        const bool todo = v < a.V && !((done >> lane) & 1u);
+        examined += todo;
+        uint32_t parent = 0xffffffffu;
+        // the first in-edge is held in HBM, vertex-indexed (a coalesced read;
+        // a vertex without in-edges holds its own id, never in the frontier):
+        // most unreached vertices find their parent there and read nothing else
+        bool head_hit = false;
+        if (todo && a.in_heads) {
             const uint32_t u = edge_word(a.in_heads, v, a.in_ebits);
-            if ((a.bitmap_in[u >> 5] >> (u & 31)) & 1u) nv = a.val[u] + 1;
-            h = b + 1;
+            head_hit = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
+            if (head_hit) parent = u;
         }
-        if (nv == 0xffffffffu) {
+        uint32_t h = 0, e = 0;
+        if (todo && !head_hit) {
+            h = a.in_ptr[v];
+            e = a.in_ptr[v + 1];
+            if (a.in_heads && h < e) h++;  // the head was in-edge h
+        }
+        if (parent == 0xffffffffu) {
             for (uint32_t i = h; i < e; i += kBuUnroll) {
                 uint32_t u[kBuUnroll];
                 bool in[kBuUnroll];
@@ -564,15 +573,23 @@ __global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_
                 for (int k = kBuUnroll - 1; k >= 0; k--)
                     if (in[k]) hit = k;
                 if (hit >= 0) {
-                    nv = a.val[u[hit]] + 1;
+                    parent = u[hit];
                     scanned += (i - h) + (uint32_t)hit + 1;
                     break;
                 }
             }
-            if (nv == 0xffffffffu) scanned += e - h;
+            if (parent == 0xffffffffu) scanned += e - h;
         }
-        const bool won = nv != 0xffffffffu;
+        const bool won = parent != 0xffffffffu;
         const unsigned found = __ballot_sync(kFull, won);
+        // every frontier vertex holds the same value (the step is level-
+        // synchronous): one lane reads its parent's, the warp shares it
+        uint32_t nv = 0;
+        if (found) {
+            const int leader = __ffs(found) - 1;
+            if ((int)lane == leader) nv = a.val[parent] + 1;
+            nv = __shfl_sync(kFull, nv, leader);
+        }
         if (won) a.val[v] = nv;
         if (lane == 0 && found) {
             a.visited[w] = vis | found;
@@ -581,9 +598,15 @@ __global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_
         count_next(a, won, v, s_next);
     }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) scanned += __shfl_down_sync(kFull, scanned, d);
+    for (int d = 16; d > 0; d >>= 1) {
+        scanned += __shfl_down_sync(kFull, scanned, d);
+        examined += __shfl_down_sync(kFull, examined, d);
+    }
     if (lane == 0 && scanned) atomicAdd(&s_scanned, scanned);
+    if (lane == 0 && examined) atomicAdd(&s_examined, examined);
     flush_next(a, s_next);
+    if (threadIdx.x == 0 && s_examined)
+        atomicAdd((unsigned long long *)(a.stats + (CTL_BU_VERTS - CTL_STATS) / 2), s_examined);
     // in-edges are read in place from host memory (resident only on a graph
     // without a cap): the run's on-demand edges and its bottom-up edges
     if (threadIdx.x == 0 && s_scanned) {
@@ -836,6 +859,45 @@ __global__ void reached_kernel(const uint32_t *val, const uint32_t *ptr, uint32_
         edges += __shfl_down_sync(kFull, edges, d);
     }
     if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], cnt);
+        atomicAdd(&out[1], edges);
+    }
+}
+
+// BFS: reached vertices are the reached-vertex bitmap's bits (no level read).
+// A warp takes kReachedWords consecutive 32-vertex words at a time, lane =
+// vertex: all of their bitmap words and then all the offsets of their reached
+// vertices are loaded before any is summed, so each warp keeps several
+// independent loads in flight instead of a chain per word.
+constexpr int kReachedWords = 4;
+
+__global__ void reached_bits_kernel(const uint32_t *visited, const uint32_t *ptr, uint32_t V, uint32_t nwords,
+                                    unsigned long long *out) {
+    unsigned long long cnt = 0, edges = 0;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t w0 = kReachedWords * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); w0 < nwords;
+         w0 += kReachedWords * warps) {
+        uint32_t bits[kReachedWords], lo[kReachedWords], hi[kReachedWords];
+#pragma unroll
+        for (int k = 0; k < kReachedWords; k++) bits[k] = w0 + k < nwords ? visited[w0 + k] : 0u;
+#pragma unroll
+        for (int k = 0; k < kReachedWords; k++) {
+            const uint32_t v = 32 * (w0 + k) + lane;
+            const bool in = ((bits[k] >> lane) & 1u) && v < V;
+            lo[k] = in ? ptr[v] : 0u;
+            hi[k] = in ? ptr[v + 1] : 0u;
+            cnt += in;
+        }
+#pragma unroll
+        for (int k = 0; k < kReachedWords; k++) edges += hi[k] - lo[k];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        cnt += __shfl_down_sync(kFull, cnt, d);
+        edges += __shfl_down_sync(kFull, edges, d);
+    }
+    if (lane == 0 && (cnt | edges)) {
         atomicAdd(&out[0], cnt);
         atomicAdd(&out[1], edges);
     }
@@ -1359,6 +1421,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
         a.in_edges = ws->in_edges ? ws->in_edges : g->d_host_in_edges;
         a.in_resident = ws->in_edges != nullptr;
         a.in_heads = g->in_heads_ready ? g->d_in_heads : nullptr;
+        a.in_none = ws->in_none;
         a.in_ebits = g->in_ebits;
         a.bu_div = ws->tune.bu_div;
     }
@@ -1947,7 +2010,8 @@ void free_ws_buffers(Workspace *ws) {
                     (void *)ws->queue[0],
                     (void *)ws->queue[1],
                     (void *)ws->segs[0], (void *)ws->segs[1], (void *)ws->ctl, (void *)ws->huge_list, ws->pr_rank,
-                    ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum, (void *)ws->in_ptr, (void *)ws->in_edges})
+                    ws->pr_contrib[0], ws->pr_contrib[1], ws->pr_sum, (void *)ws->in_ptr, (void *)ws->in_edges,
+                    (void *)ws->in_none})
         if (p) cudaFree(p);
     if (ws->h_ctl) cudaFreeHost(ws->h_ctl);
     for (void *p : {(void *)ws->g_stage, (void *)ws->g_items})
@@ -2128,6 +2192,16 @@ asc_status ensure_in_ptr(asc_graph *g) {
     ASC_CUDA(cudaMalloc(&ws->in_ptr, 4 * (g->V + 1)));
     ASC_CUDA(cudaMemcpy(ws->in_ptr, g->h_in_ptr, 4 * (g->V + 1), cudaMemcpyHostToDevice));
     ws->device_bytes += 4 * (g->V + 1);
+    {
+        // one bit per vertex without in-edges (bits past V set: nothing to look for there)
+        const uint64_t nw = g->V / 32 + 2;
+        std::vector<uint32_t> none(nw, 0);
+        for (uint64_t v = 0; v < 32 * nw; v++)
+            if (v >= g->V || g->h_in_ptr[v + 1] == g->h_in_ptr[v]) none[v >> 5] |= 1u << (v & 31);
+        ASC_CUDA(cudaMalloc(&ws->in_none, 4 * nw));
+        ASC_CUDA(cudaMemcpy(ws->in_none, none.data(), 4 * nw, cudaMemcpyHostToDevice));
+        ws->device_bytes += 4 * nw;
+    }
     if (g->static_edges >= g->E) {
         const uint64_t words = g->in_ebits == 32 ? std::max<uint64_t>(1, g->E) : (g->E * g->in_ebits + 31) / 32 + 1;
         ASC_CUDA(cudaMalloc(&ws->in_edges, 4 * words));
@@ -2340,8 +2414,12 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     // so count them
     const bool count_reached = algo == ASC_SSSP || (algo == ASC_BFS && ws->bu_active);
     if (count_reached) {
-        reached_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(ws->val, g->d_ptr, V,
-                                                           (unsigned long long *)(ws->ctl + CTL_STATS) + 4);
+        if (algo == ASC_BFS)
+            reached_bits_kernel<<<fill_grid(ws, 32ull * nwords), kBlock, 0, s>>>(
+                ws->visited, g->d_ptr, V, nwords, (unsigned long long *)(ws->ctl + CTL_STATS) + 4);
+        else
+            reached_kernel<<<fill_grid(ws, V), kBlock, 0, s>>>(ws->val, g->d_ptr, V,
+                                                               (unsigned long long *)(ws->ctl + CTL_STATS) + 4);
         launches++;
     }
     ASC_CUDA(cudaEventRecord(ws->ev[1], s));
@@ -2354,7 +2432,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
     ASC_CUDA(cudaEventRecord(ws->ev[2], s));
     ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_STATS, ws->ctl + CTL_STATS, 4 * (CTL_BODIES + 1 - CTL_STATS),
                              cudaMemcpyDeviceToHost, s));
-    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_BU_EDGES, ws->ctl + CTL_BU_EDGES, 8, cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaMemcpyAsync(ws->h_ctl + CTL_BU_EDGES, ws->ctl + CTL_BU_EDGES, 16, cudaMemcpyDeviceToHost, s));
     ASC_CUDA(cudaStreamSynchronize(s));
     if (use_graph) {
         iters = (int)ws->h_ctl[CTL_ITERS];
@@ -2378,6 +2456,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
             st->staged_chunks = part_copies;
         }
         st->bottom_up_edges = bu_edges;
+        st->bottom_up_vertices = *(const unsigned long long *)(ws->h_ctl + CTL_BU_VERTS);
         st->frontier_vertices = hs[2] + hs[3];
         st->ondemand_vertices = hs[3];
         if (algo == ASC_CC) {
@@ -3326,7 +3405,7 @@ uint64_t workspace_bytes(asc_graph *g, bool pagerank) {
     if (pagerank && (!g->ws || !g->ws->pr_rank)) b += 4ull * 8 * V;
     // in-edge offsets of bottom-up BFS steps, allocated on the first BFS
     const uint32_t bu = g->ws ? g->ws->tune.bu_div : (g->has_tuning ? g->tuning.bu_div : Tuning().bu_div);
-    if (!g->is_csc && bu && (!g->ws || !g->ws->in_ptr)) b += 4 * (V + 1);
+    if (!g->is_csc && bu && (!g->ws || !g->ws->in_ptr)) b += 4 * (V + 1) + 4 * (V / 32 + 2);
     return b;
 }
 

@@ -723,11 +723,12 @@ asc_status build_in_edges(asc_graph *g) {
     g->h_in_edges = packed;
     g->d_host_in_edges = (const uint32_t *)dp;
     if (g->d_in_heads && !g->in_heads_ready) {
-        // first in-edge of every vertex (0 where it has none), vertex-indexed
+        // first in-edge of every vertex, vertex-indexed; a vertex without
+        // in-edges holds its own id (never a frontier vertex when it is probed,
+        // since only unreached vertices probe)
         std::vector<uint32_t> first(V ? V : 1, 0);
         parallel_for(V, host_threads(V), [&](unsigned, uint64_t b, uint64_t e) {
-            for (uint64_t v = b; v < e; v++)
-                if (in_ptr[v + 1] > in_ptr[v]) first[v] = raw[in_ptr[v]];
+            for (uint64_t v = b; v < e; v++) first[v] = in_ptr[v + 1] > in_ptr[v] ? raw[in_ptr[v]] : (uint32_t)v;
         });
         uint32_t *hp = nullptr;
         ASC_TRY(pack_stream(first.data(), V, bits, &hp));

@@ -198,6 +198,7 @@ typedef struct asc_stats {
                                     ondemand_bytes then counts the bytes those copies moved */
     uint64_t bottom_up_edges;    /* BFS: in-edges read by bottom-up steps (counted in ondemand_edges) */
     double ms_bottom_up;         /* with ASC_RUN_PHASE_TIMING: bottom-up BFS kernels */
+    uint64_t bottom_up_vertices; /* BFS: unreached vertices the bottom-up steps examined */
 } asc_stats;
 
 /* ---- status and errors -------------------------------------------------- */
