@@ -523,7 +523,15 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
 // pinned host memory, kBuUnroll per lane before any frontier probe.
 constexpr int kBuUnroll = 4;
 
-__global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_t nwords) {
+// Words a warp takes per pass: all of their bitmap words, heads and frontier
+// probes are loaded before any is used, so a warp keeps that many independent
+// load chains in flight.
+constexpr int kBuWords = 4;
+// CTAs per SM the bottom-up kernel is compiled for (38 registers, no spill at
+// 4 words per pass); its grid is one wave of them.
+constexpr int kBuMinBlocks = 6;
+
+__global__ void __launch_bounds__(kBlock, kBuMinBlocks) bottom_up_kernel(RegionArgs a, uint32_t nwords) {
     if (!bottom_up_step(a)) return;
     __shared__ uint32_t s_next[2];
     __shared__ unsigned long long s_scanned, s_examined;
@@ -533,69 +541,82 @@ __global__ void __launch_bounds__(kBlock) bottom_up_kernel(RegionArgs a, uint32_
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (kBlock / 32);
     unsigned long long scanned = 0, examined = 0;
-    for (uint32_t w = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); w < nwords; w += warps) {
-        const uint32_t vis = a.visited[w];
+    for (uint32_t w0 = kBuWords * (blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5)); w0 < nwords;
+         w0 += kBuWords * warps) {
         // vertices without in-edges can never be reached: about half of an
         // RMAT graph, nearly all of its unreachable vertices
-        const uint32_t done = vis | a.in_none[w];
-        if (done == 0xffffffffu) continue;  // the whole warp: nothing to look for in this word
-        const uint32_t v = 32 * w + lane;
-        const bool todo = v < a.V && !((done >> lane) & 1u);
-        examined += todo;
-        uint32_t parent = 0xffffffffu;
+        uint32_t vis[kBuWords], done[kBuWords];
+#pragma unroll
+        for (int k = 0; k < kBuWords; k++) {
+            const bool in = w0 + k < nwords;
+            vis[k] = in ? a.visited[w0 + k] : 0xffffffffu;
+            done[k] = in ? vis[k] | a.in_none[w0 + k] : 0xffffffffu;
+        }
         // the first in-edge is held in HBM, vertex-indexed (a coalesced read;
         // a vertex without in-edges holds its own id, never in the frontier):
         // most unreached vertices find their parent there and read nothing else
-        bool head_hit = false;
-        if (todo && a.in_heads) {
-            const uint32_t u = edge_word(a.in_heads, v, a.in_ebits);
-            head_hit = (a.bitmap_in[u >> 5] >> (u & 31)) & 1u;
-            if (head_hit) parent = u;
+        uint32_t head[kBuWords];
+        bool todo[kBuWords], hit[kBuWords];
+#pragma unroll
+        for (int k = 0; k < kBuWords; k++) {
+            const uint32_t v = 32 * (w0 + k) + lane;
+            todo[k] = done[k] != 0xffffffffu && v < a.V && !((done[k] >> lane) & 1u);
+            head[k] = todo[k] && a.in_heads ? edge_word(a.in_heads, v, a.in_ebits) : 0u;
         }
-        uint32_t h = 0, e = 0;
-        if (todo && !head_hit) {
-            h = a.in_ptr[v];
-            e = a.in_ptr[v + 1];
-            if (a.in_heads && h < e) h++;  // the head was in-edge h
-        }
-        if (parent == 0xffffffffu) {
-            for (uint32_t i = h; i < e; i += kBuUnroll) {
-                uint32_t u[kBuUnroll];
-                bool in[kBuUnroll];
 #pragma unroll
-                for (int k = 0; k < kBuUnroll; k++)
-                    u[k] = i + k < e ? edge_word(a.in_edges, (uint64_t)i + k, a.in_ebits) : 0xffffffffu;
+        for (int k = 0; k < kBuWords; k++)
+            hit[k] = todo[k] && a.in_heads && ((a.bitmap_in[head[k] >> 5] >> (head[k] & 31)) & 1u);
 #pragma unroll
-                for (int k = 0; k < kBuUnroll; k++)
-                    in[k] = u[k] != 0xffffffffu && ((a.bitmap_in[u[k] >> 5] >> (u[k] & 31)) & 1u);
-                int hit = -1;
-#pragma unroll
-                for (int k = kBuUnroll - 1; k >= 0; k--)
-                    if (in[k]) hit = k;
-                if (hit >= 0) {
-                    parent = u[hit];
-                    scanned += (i - h) + (uint32_t)hit + 1;
-                    break;
-                }
+        for (int k = 0; k < kBuWords; k++) {
+            if (done[k] == 0xffffffffu) continue;  // the whole warp: nothing to look for in this word
+            const uint32_t w = w0 + k, v = 32 * w + lane;
+            examined += todo[k];
+            uint32_t parent = hit[k] ? head[k] : 0xffffffffu;
+            uint32_t h = 0, e = 0;
+            if (todo[k] && !hit[k]) {
+                h = a.in_ptr[v];
+                e = a.in_ptr[v + 1];
+                if (a.in_heads && h < e) h++;  // the head was in-edge h
             }
-            if (parent == 0xffffffffu) scanned += e - h;
+            if (parent == 0xffffffffu) {
+                for (uint32_t i = h; i < e; i += kBuUnroll) {
+                    uint32_t u[kBuUnroll];
+                    bool in[kBuUnroll];
+#pragma unroll
+                    for (int q = 0; q < kBuUnroll; q++)
+                        u[q] = i + q < e ? edge_word(a.in_edges, (uint64_t)i + q, a.in_ebits) : 0xffffffffu;
+#pragma unroll
+                    for (int q = 0; q < kBuUnroll; q++)
+                        in[q] = u[q] != 0xffffffffu && ((a.bitmap_in[u[q] >> 5] >> (u[q] & 31)) & 1u);
+                    int at = -1;
+#pragma unroll
+                    for (int q = kBuUnroll - 1; q >= 0; q--)
+                        if (in[q]) at = q;
+                    if (at >= 0) {
+                        parent = u[at];
+                        scanned += (i - h) + (uint32_t)at + 1;
+                        break;
+                    }
+                }
+                if (parent == 0xffffffffu) scanned += e - h;
+            }
+            const bool won = parent != 0xffffffffu;
+            const unsigned found = __ballot_sync(kFull, won);
+            // every frontier vertex holds the same value (the step is level-
+            // synchronous): one lane reads its parent's, the warp shares it
+            uint32_t nv = 0;
+            if (found) {
+                const int leader = __ffs(found) - 1;
+                if ((int)lane == leader) nv = a.val[parent] + 1;
+                nv = __shfl_sync(kFull, nv, leader);
+            }
+            if (won) a.val[v] = nv;
+            if (lane == 0 && found) {
+                a.visited[w] = vis[k] | found;
+                a.bitmap[w] = found;
+            }
+            count_next(a, won, v, s_next);
         }
-        const bool won = parent != 0xffffffffu;
-        const unsigned found = __ballot_sync(kFull, won);
-        // every frontier vertex holds the same value (the step is level-
-        // synchronous): one lane reads its parent's, the warp shares it
-        uint32_t nv = 0;
-        if (found) {
-            const int leader = __ffs(found) - 1;
-            if ((int)lane == leader) nv = a.val[parent] + 1;
-            nv = __shfl_sync(kFull, nv, leader);
-        }
-        if (won) a.val[v] = nv;
-        if (lane == 0 && found) {
-            a.visited[w] = vis | found;
-            a.bitmap[w] = found;
-        }
-        count_next(a, won, v, s_next);
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -1477,6 +1498,12 @@ uint32_t grid_for(const Workspace *ws, uint64_t work_items) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(cap, work_items));
 }
 
+// One wave of bottom-up CTAs (a warp per kBuWords bitmap words per pass).
+uint32_t bu_grid(const Workspace *ws, uint64_t nwords) {
+    const uint64_t blocks = (nwords + kBuWords * (kBlock / 32) - 1) / (kBuWords * (kBlock / 32));
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)ws->num_sms * kBuMinBlocks));
+}
+
 uint32_t fill_grid(const Workspace *ws, uint64_t n) {
     uint64_t blocks = (n + kBlock - 1) / kBlock;
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)ws->num_sms * 8));
@@ -1616,7 +1643,7 @@ asc_status build_loop_graph(asc_graph *g, asc_algo algo, uint32_t cap) {
                     if (near_far(g, algo)) cudaMemsetAsync(ws->ctl + CTL_MINFAR, 0xff, 4, cs);
                     fused(cs, x, grid);
                     if (algo == ASC_BFS && x.r0.in_ptr)
-                        bottom_up_kernel<<<fill_grid(ws, 32ull * (V / 32 + 1)), kBlock, 0, cs>>>(x.r0, V / 32 + 1);
+                        bottom_up_kernel<<<bu_grid(ws, V / 32 + 1), kBlock, 0, cs>>>(x.r0, V / 32 + 1);
                     if (near_far(g, algo)) launch_far(g, cs, x.r0);
                     build_frontier_kernel<<<fill_grid(ws, V / 32 + 1), kBlock, 0, cs>>>(x.r0, ws->bitmap[po],
                                                                                         V / 32 + 1);
@@ -2358,7 +2385,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
             RegionArgs a = region_args(g, parity, 0, false);
             ASC_TRY(pt.begin(2));
             pt.record(s);
-            bottom_up_kernel<<<fill_grid(ws, 32ull * nwords), kBlock, 0, s>>>(a, nwords);
+            bottom_up_kernel<<<bu_grid(ws, nwords), kBlock, 0, s>>>(a, nwords);
             pt.record(s);
             launches++;
         } else if (pt.on) {
@@ -2387,7 +2414,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
             fused(s, x, grid_for(ws, items));
             launches++;
             if (algo == ASC_BFS && x.r0.in_ptr) {
-                bottom_up_kernel<<<fill_grid(ws, 32ull * nwords), kBlock, 0, s>>>(x.r0, nwords);
+                bottom_up_kernel<<<bu_grid(ws, nwords), kBlock, 0, s>>>(x.r0, nwords);
                 launches++;
             }
         }
