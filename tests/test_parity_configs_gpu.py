@@ -132,9 +132,12 @@ def test_static_split_modes_follow_reference_rule(packing, monkeypatch):
         assert g.info.static_edges % 4096 == 0 and g.info.static_edges <= E
 
 
-@pytest.mark.parametrize("frac", [1.0, 0.3, 0.0])
-def test_reference_pagerank_scale16(frac):
-    cptr, ccol, od = A.rmat_csr(16, 16, 3, transpose=True)
+@pytest.mark.parametrize("scale,frac", [(16, 1.0), (16, 0.3), (16, 0.0), (20, 0.3)])
+def test_reference_pagerank_at_scale(scale, frac):
+    """Reference PageRank's per-vertex stop (|delta| <= 0.001, vertices stay
+    inactive) makes a wrong pass count visible: the engine's pass count and
+    every rank match the oracle's at RMAT scale 16 and 20 (1 M vertices)."""
+    cptr, ccol, od = A.rmat_csr(scale, 16, 3, transpose=True)
     exp, passes = oracle.pr_ref(cptr, ccol, od)
     with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=frac)) as g:
         got, st = g.run("pr")
