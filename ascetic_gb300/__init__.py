@@ -99,7 +99,9 @@ class ServerStats(ctypes.Structure):
                 ("cancelled", ctypes.c_uint64), ("batch_iterations", ctypes.c_uint64),
                 ("device_bytes", ctypes.c_uint64), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
                 ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double),
-                ("span_s", ctypes.c_double)]
+                ("span_s", ctypes.c_double), ("engines_created", ctypes.c_uint64),
+                ("engines_freed", ctypes.c_uint64), ("workspaces_freed", ctypes.c_uint64),
+                ("memory_waits", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

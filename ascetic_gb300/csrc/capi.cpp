@@ -150,9 +150,11 @@ asc_status asc_run(asc_graph *g, asc_algo algo, uint32_t source, const asc_param
         if (p.pr_mode == ASC_PR_REF && p.precision != ASC_F64)
             return fail(ASC_ERR_UNSUPPORTED, "the reference PageRank runs in FP64 only");
         if (!(p.damping > 0 && p.damping < 1)) return fail(ASC_ERR_INVALID, "damping must be in (0, 1)");
-        return run_pagerank(g, p, out, stats);
+        ASC_TRY(run_pagerank(g, p, out, stats));
+        return self_check_result();
     }
-    return run_traversal(g, algo, source, p, out, stats);
+    ASC_TRY(run_traversal(g, algo, source, p, out, stats));
+    return self_check_result();
 }
 
 asc_status asc_run_batch(asc_graph *g, asc_algo algo, const uint32_t *sources, uint32_t n,

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -118,6 +119,19 @@ struct asc_graph {
     uint64_t stage_words = 0;      // u32 words in each staging buffer (0: no staging)
     // in-edges of a CSR graph (bottom-up BFS steps), built on first use
     uint32_t *h_in_ptr = nullptr;  // V+1 offsets (host)
+    uint32_t *h_in_none = nullptr;  // V/32+2 words: bit set where a vertex has no in-edges (host)
+    // lists cut into segments for a (huge_degree, segment_edges), found on the
+    // first workspace of that tuning and reused by later ones (a server frees
+    // and re-creates the workspaces of idle graphs and batches, whose tunings
+    // differ); the most recent few tunings are kept
+    struct LongLists {
+        uint32_t huge_degree = 0, segment_edges = 0;
+        std::vector<uint32_t> list, bits;  // long-list vertices; one bit per vertex (V/32+2 words)
+        uint64_t seg_static = 0, seg_ondemand = 0;  // segments of the static / on-demand long lists
+        uint32_t n_static = 0;
+    };
+    std::vector<LongLists> long_lists;
+    std::mutex long_lists_mu;
     uint32_t *h_in_edges = nullptr;  // source ids, a bit stream of in_ebits per edge (pinned, mapped)
     const uint32_t *d_host_in_edges = nullptr;
     uint32_t in_ebits = 32;
@@ -163,6 +177,9 @@ void batch_destroy(BatchEngine *b);
 bool batch_has_plane(BatchEngine *b, uint32_t slot);
 asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source);
 bool batch_busy(const BatchEngine *b);
+void batch_abort(BatchEngine *b);
+// Self-checking build (ASC_SELF_CHECK): the first failed device index check since the last call.
+asc_status self_check_result();
 // Source slots of a batch: 64, or the row width of a narrower SSSP batch.
 uint32_t batch_slots(const BatchEngine *b);
 asc_status batch_launch(BatchEngine *b);

@@ -64,6 +64,23 @@ constexpr unsigned kFull = 0xffffffffu;
 #endif
 constexpr int kWarps = kBlock / 32;
 
+// Self-checking build (nvcc -DASC_SELF_CHECK): indices the kernels take from
+// device data (frontier lists, segment items, decoded edges, level-plane
+// pointers, list and segment capacities) are checked before use; the first bad
+// one is recorded as (site << 32 | index), its access is skipped, and the run
+// or batch iteration that launched the kernel fails with ASC_ERR_CUDA naming
+// the site. Without the macro the checks compile to nothing.
+#ifdef ASC_SELF_CHECK
+__device__ unsigned long long g_self_check;
+__device__ __noinline__ bool self_check_fail(uint32_t site, uint64_t idx) {
+    atomicCAS(&g_self_check, 0ull, ((unsigned long long)site << 32) | (idx & 0xffffffffull));
+    return true;
+}
+#define ASC_BAD(cond, site, idx) ((cond) ? self_check_fail((site), (idx)) : false)
+#else
+#define ASC_BAD(cond, site, idx) false
+#endif
+
 enum Alg { kBFS = 0, kSSSP = 1, kCC = 2 };
 
 // Control block (u32 words). Per parity p: [8p+0..3] counts of the frontier
@@ -105,6 +122,7 @@ struct RegionArgs {
     uint32_t huge;
     uint32_t seg_len;
     uint32_t segcap_static;
+    uint32_t segcap_ondemand;
     uint32_t V;
     uint32_t dense_div;
     uint32_t wbits;               // > 0: u32 edges packed as (dst << wbits) | weight
@@ -305,6 +323,7 @@ constexpr int kUnroll = ASC_EXPAND_UNROLL;
 template <int ALG, int WORDS>
 __device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem &sm, uint32_t *s_next) {
     uint32_t deg = 0, start = 0, vu = 0;
+    if (act && ASC_BAD(u >= a.V, 1, u)) act = false;
     if (act) {
         start = a.ptr[u];
         deg = a.ptr[u + 1] - start;
@@ -337,6 +356,10 @@ __device__ void expand_vertices(const RegionArgs &a, bool act, uint32_t u, Smem 
                     else hi = mid;
                 }
                 load_edge<ALG, WORDS>(a, sm.vu[lo], (uint64_t)sm.start[lo] + (e - sm.pref[lo]), v[k], nv[k]);
+                if (ASC_BAD(v[k] >= a.V, 2, v[k])) {
+                    v[k] = 0;
+                    nv[k] = 0xffffffffu;
+                }
             }
         }
     };
@@ -389,6 +412,7 @@ __device__ __forceinline__ void expand_tile(const RegionArgs &a, uint32_t tile, 
 template <int ALG, int WORDS>
 __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_next) {
     const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+    if (ASC_BAD(u >= a.V, 3, u)) return;
     const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
     const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
@@ -401,6 +425,10 @@ __device__ void expand_segment(const RegionArgs &a, uint64_t item, uint32_t *s_n
             v[k] = 0;
             nv[k] = 0xffffffffu;
             if (j < n) load_edge<ALG, WORDS>(a, vu, b + j, v[k], nv[k]);
+            if (j < n && ASC_BAD(v[k] >= a.V, 2, v[k])) {
+                v[k] = 0;
+                nv[k] = 0xffffffffu;
+            }
         }
     };
     for (uint32_t base = 0; base < n; base += kUnroll * kBlock) {
@@ -562,6 +590,7 @@ __global__ void __launch_bounds__(kBlock, kBuMinBlocks) bottom_up_kernel(RegionA
             const uint32_t v = 32 * (w0 + k) + lane;
             todo[k] = done[k] != 0xffffffffu && v < a.V && !((done[k] >> lane) & 1u);
             head[k] = todo[k] && a.in_heads ? edge_word(a.in_heads, v, a.in_ebits) : 0u;
+            if (ASC_BAD(head[k] >= a.V, 16, head[k])) head[k] = v;
         }
 #pragma unroll
         for (int k = 0; k < kBuWords; k++)
@@ -583,8 +612,10 @@ __global__ void __launch_bounds__(kBlock, kBuMinBlocks) bottom_up_kernel(RegionA
                     uint32_t u[kBuUnroll];
                     bool in[kBuUnroll];
 #pragma unroll
-                    for (int q = 0; q < kBuUnroll; q++)
+                    for (int q = 0; q < kBuUnroll; q++) {
                         u[q] = i + q < e ? edge_word(a.in_edges, (uint64_t)i + q, a.in_ebits) : 0xffffffffu;
+                        if (u[q] != 0xffffffffu && ASC_BAD(u[q] >= a.V, 17, u[q])) u[q] = 0xffffffffu;
+                    }
 #pragma unroll
                     for (int q = 0; q < kBuUnroll; q++)
                         in[q] = u[q] != 0xffffffffu && ((a.bitmap_in[u[q] >> 5] >> (u[q] & 31)) & 1u);
@@ -711,6 +742,7 @@ __global__ void build_frontier_kernel(RegionArgs a, const uint32_t *next_bits, u
             const uint32_t nseg = (deg + a.seg_len - 1) / a.seg_len;
             const bool od = v >= a.S;
             const uint32_t sb = atomicAdd(&a.cnt_out[2 + od], nseg);
+            if (ASC_BAD((uint64_t)sb + nseg > (od ? a.segcap_ondemand : a.segcap_static), 13, sb)) continue;
             uint64_t *dst = a.seg_out + (od ? a.segcap_static : 0) + sb;
             for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
         }
@@ -744,13 +776,15 @@ __global__ void build_frontier_kernel(RegionArgs a, const uint32_t *next_bits, u
         while (x) {
             const int b = __ffs(x) - 1;
             x &= x - 1;
-            a.q_out[b0++] = v0 + b;
+            if (!ASC_BAD(b0 >= a.S, 14, b0)) a.q_out[b0] = v0 + b;
+            b0++;
         }
         x = w1;
         while (x) {
             const int b = __ffs(x) - 1;
             x &= x - 1;
-            a.q_out[a.S + b1++] = v0 + b;
+            if (!ASC_BAD(a.S + b1 >= a.V, 15, b1)) a.q_out[a.S + b1] = v0 + b;
+            b1++;
         }
     }
 }
@@ -1033,6 +1067,12 @@ __device__ __forceinline__ void block_reduce2_atomic(double a, double b, double 
     __syncthreads();
 }
 
+// Edges per thread per pass of the PageRank pull (all reads issued first).
+#ifndef ASC_PR_UNROLL
+#define ASC_PR_UNROLL 4
+#endif
+constexpr int kPrUnroll = ASC_PR_UNROLL;
+
 template <typename T>
 struct PrSmem {
     uint32_t pref[kBlock + 1];
@@ -1066,32 +1106,52 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
     if (threadIdx.x == 0) sm.pref[kBlock] = total;
     const uint32_t nact = __syncthreads_count(valid && !huge);
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = 0; base < total; base += kBlock) {
-        const uint32_t e = base + threadIdx.x;
-        T x = (T)0;
-        int owner = -1 - lane;  // distinct per invalid lane
-        if (e < total) {
-            int lo = 0, hi = kBlock;
-            while (hi - lo > 1) {
-                int mid = (lo + hi) >> 1;
-                if (sm.pref[mid] <= e) lo = mid;
-                else hi = mid;
-            }
-            owner = lo;
-            const uint32_t srcv = edge_word(a.edges, (uint64_t)sm.start[lo] + (e - sm.pref[lo]), a.ebits);
-            x = p.c_old[srcv];
-        }
-        // segmented suffix sum over lanes with the same owner (owners ascend
-        // with the lane; a fixed shuffle tree, so the same edges give the same
-        // partial every pass)
+    // kPrUnroll edges per thread per pass (edge k of a pass is edge
+    // base + k * kBlock + thread): every source id is loaded, then every
+    // contribution gathered, before any is summed, so a thread has kPrUnroll
+    // reads in flight over the host link (on-demand region) instead of one
+    for (uint32_t base = 0; base < total; base += kPrUnroll * kBlock) {
+        T x[kPrUnroll];
+        int owner[kPrUnroll];
+        uint32_t srcv[kPrUnroll];
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            T y = __shfl_down_sync(kFull, x, d);
-            int oy = __shfl_down_sync(kFull, owner, d);
-            if (lane + d < 32 && oy == owner) x += y;
+        for (int k = 0; k < kPrUnroll; k++) {
+            const uint32_t e = base + k * kBlock + threadIdx.x;
+            owner[k] = -1 - lane;  // distinct per invalid lane
+            srcv[k] = 0xffffffffu;
+            if (e < total) {
+                int lo = 0, hi = kBlock;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (sm.pref[mid] <= e) lo = mid;
+                    else hi = mid;
+                }
+                owner[k] = lo;
+                srcv[k] = edge_word(a.edges, (uint64_t)sm.start[lo] + (e - sm.pref[lo]), a.ebits);
+                if (ASC_BAD(srcv[k] >= a.V, 21, srcv[k])) {
+                    srcv[k] = 0xffffffffu;
+                    owner[k] = -1 - lane;
+                }
+            }
         }
-        int oprev = __shfl_up_sync(kFull, owner, 1);
-        if (owner >= 0 && (lane == 0 || oprev != owner)) atomicAdd(&sm.sum[owner], PrAcc<T>::from(x));
+#pragma unroll
+        for (int k = 0; k < kPrUnroll; k++) x[k] = srcv[k] != 0xffffffffu ? p.c_old[srcv[k]] : (T)0;
+#pragma unroll
+        for (int k = 0; k < kPrUnroll; k++) {
+            // segmented suffix sum over lanes with the same owner (owners
+            // ascend with the lane; a fixed shuffle tree, so the same edges
+            // give the same partial every pass)
+            T xs = x[k];
+            const int ow = owner[k];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                T y = __shfl_down_sync(kFull, xs, d);
+                int oy = __shfl_down_sync(kFull, ow, d);
+                if (lane + d < 32 && oy == ow) xs += y;
+            }
+            int oprev = __shfl_up_sync(kFull, ow, 1);
+            if (ow >= 0 && (lane == 0 || oprev != ow)) atomicAdd(&sm.sum[ow], PrAcc<T>::from(xs));
+        }
     }
     __syncthreads();
     double res = 0, dang = 0;
@@ -1144,7 +1204,22 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     T x = (T)0;  // this thread's edges in order, then a fixed warp tree
-    for (uint32_t j = threadIdx.x; j < n; j += kBlock) x += p.c_old[edge_word(a.edges, b + j, a.ebits)];
+    for (uint32_t j0 = threadIdx.x; j0 < n; j0 += kPrUnroll * kBlock) {
+        // kPrUnroll loads in flight, added in edge order
+        uint32_t sv[kPrUnroll];
+#pragma unroll
+        for (int k = 0; k < kPrUnroll; k++) {
+            const uint32_t j = j0 + k * kBlock;
+            sv[k] = j < n ? edge_word(a.edges, b + j, a.ebits) : 0xffffffffu;
+            if (sv[k] != 0xffffffffu && ASC_BAD(sv[k] >= a.V, 21, sv[k])) sv[k] = 0xffffffffu;
+        }
+        T c[kPrUnroll];
+#pragma unroll
+        for (int k = 0; k < kPrUnroll; k++) c[k] = sv[k] != 0xffffffffu ? p.c_old[sv[k]] : (T)0;
+#pragma unroll
+        for (int k = 0; k < kPrUnroll; k++)
+            if (sv[k] != 0xffffffffu) x += c[k];
+    }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(kFull, x, d);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1331,6 +1406,7 @@ __global__ void seed_huge_segments_kernel(RegionArgs a, const uint32_t *huge_lis
         const uint32_t nseg = (deg + a.seg_len - 1) / a.seg_len;
         const bool od = i >= n_static;
         const uint32_t base = atomicAdd(&a.cnt_out[2 + od], nseg);
+        if (ASC_BAD((uint64_t)base + nseg > (od ? a.segcap_ondemand : a.segcap_static), 20, base)) continue;
         uint64_t *dst = a.seg_out + (od ? a.segcap_static : 0) + base;
         for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
     }
@@ -1354,20 +1430,36 @@ asc_status alloc_workspace(asc_graph *g, Workspace *ws, bool graph_tuning = true
     const uint64_t V = g->V;
     const uint32_t S = g->static_vertices;
     const Tuning &t = ws->tune;
-    uint64_t cs = 0, co = 0;
-    std::vector<uint32_t> huge;
-    for (uint64_t v = 0; v < V; v++) {
-        uint32_t d = g->h_ptr[v + 1] - g->h_ptr[v];
-        if (d > t.huge_degree) {
-            uint64_t ns = (d + t.segment_edges - 1) / t.segment_edges;
-            if (v < S) { cs += ns; ws->n_huge_static++; }
-            else co += ns;
-            huge.push_back((uint32_t)v);
+    std::lock_guard<std::mutex> plan_lk(g->long_lists_mu);
+    auto &cache = g->long_lists;
+    auto hit = std::find_if(cache.begin(), cache.end(), [&](const asc_graph::LongLists &c) {
+        return c.huge_degree == t.huge_degree && c.segment_edges == t.segment_edges;
+    });
+    if (hit == cache.end()) {
+        constexpr size_t kKeep = 4;
+        if (cache.size() >= kKeep) cache.erase(cache.begin());
+        cache.emplace_back();
+        hit = cache.end() - 1;
+        asc_graph::LongLists &ll = *hit;
+        for (uint64_t v = 0; v < V; v++) {
+            uint32_t d = g->h_ptr[v + 1] - g->h_ptr[v];
+            if (d > t.huge_degree) {
+                uint64_t ns = (d + t.segment_edges - 1) / t.segment_edges;
+                if (v < S) { ll.seg_static += ns; ll.n_static++; }
+                else ll.seg_ondemand += ns;
+                ll.list.push_back((uint32_t)v);
+            }
         }
+        ll.bits.assign(V / 32 + 2, 0);
+        for (uint32_t v : ll.list) ll.bits[v >> 5] |= 1u << (v & 31);
+        ll.huge_degree = t.huge_degree;
+        ll.segment_edges = t.segment_edges;
     }
+    const asc_graph::LongLists &ll = *hit;
+    const std::vector<uint32_t> &huge = ll.list, &hbits = ll.bits;
+    const uint64_t cs = ll.seg_static, co = ll.seg_ondemand;
+    ws->n_huge_static = ll.n_static;
     ws->n_huge_total = (uint32_t)huge.size();
-    std::vector<uint32_t> hbits(V / 32 + 2, 0);
-    for (uint32_t v : huge) hbits[v >> 5] |= 1u << (v & 31);
     ws->segcap_static = cs;
     ws->segcap_ondemand = co;
     uint64_t bytes = 0;
@@ -1451,6 +1543,7 @@ RegionArgs base_args(asc_graph *g, Workspace *ws, int parity_in) {
     a.huge = ws->tune.huge_degree;
     a.seg_len = ws->tune.segment_edges;
     a.segcap_static = (uint32_t)ws->segcap_static;
+    a.segcap_ondemand = (uint32_t)ws->segcap_ondemand;
     a.stats = (unsigned long long *)(ws->ctl + CTL_STATS);
     const int po = 1 - parity_in;
     a.cnt_in = ws->ctl + CTL_BLOCK * parity_in;
@@ -2220,13 +2313,18 @@ asc_status ensure_in_ptr(asc_graph *g) {
     ASC_CUDA(cudaMemcpy(ws->in_ptr, g->h_in_ptr, 4 * (g->V + 1), cudaMemcpyHostToDevice));
     ws->device_bytes += 4 * (g->V + 1);
     {
-        // one bit per vertex without in-edges (bits past V set: nothing to look for there)
+        // one bit per vertex without in-edges (bits past V set: nothing to look
+        // for there), built once per graph: a server that frees the state of an
+        // idle graph uploads it again
         const uint64_t nw = g->V / 32 + 2;
-        std::vector<uint32_t> none(nw, 0);
-        for (uint64_t v = 0; v < 32 * nw; v++)
-            if (v >= g->V || g->h_in_ptr[v + 1] == g->h_in_ptr[v]) none[v >> 5] |= 1u << (v & 31);
+        if (!g->h_in_none) {
+            uint32_t *none = new uint32_t[nw]();
+            for (uint64_t v = 0; v < 32 * nw; v++)
+                if (v >= g->V || g->h_in_ptr[v + 1] == g->h_in_ptr[v]) none[v >> 5] |= 1u << (v & 31);
+            g->h_in_none = none;
+        }
         ASC_CUDA(cudaMalloc(&ws->in_none, 4 * nw));
-        ASC_CUDA(cudaMemcpy(ws->in_none, none.data(), 4 * nw, cudaMemcpyHostToDevice));
+        ASC_CUDA(cudaMemcpy(ws->in_none, g->h_in_none, 4 * nw, cudaMemcpyHostToDevice));
         ws->device_bytes += 4 * nw;
     }
     if (g->static_edges >= g->E) {
@@ -2791,6 +2889,7 @@ template <int WORDS>
 __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint32_t u, MsSmem &sm) {
     uint32_t deg = 0, start = 0;
     unsigned long long f = 0;
+    if (act && ASC_BAD(u >= m.V, 4, u)) act = false;
     if (act) {
         start = a.ptr[u];
         deg = a.ptr[u + 1] - start;
@@ -2825,6 +2924,10 @@ __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
                 v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : layout_word<WORDS>(a.edges, idx, a.ebits) >> a.wbits;
                 fk[k] = sm.f[lo];
+                if (ASC_BAD(v[k] >= m.V, 5, v[k])) {
+                    v[k] = 0;
+                    fk[k] = 0;
+                }
             }
         }
 #pragma unroll
@@ -2842,6 +2945,7 @@ __device__ void ms_vertices(const MsArgs &m, const RegionArgs &a, bool act, uint
 template <int WORDS>
 __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) {
     const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+    if (ASC_BAD(u >= m.V, 6, u)) return;
     const uint32_t b0 = a.ptr[u], e0 = a.ptr[u + 1];
     const uint64_t b = (uint64_t)b0 + (uint64_t)k0 * a.seg_len;
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
@@ -2857,6 +2961,10 @@ __device__ void ms_segment(const MsArgs &m, const RegionArgs &a, uint64_t item) 
             ok[k] = j < n;
             v[k] = ok[k] ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : layout_word<WORDS>(a.edges, b + j, a.ebits) >> a.wbits)
                          : 0;
+            if (ok[k] && ASC_BAD(v[k] >= m.V, 5, v[k])) {
+                ok[k] = false;
+                v[k] = 0;
+            }
         }
 #pragma unroll
         for (int k = 0; k < kMsUnroll; k++) vis[k] = ok[k] ? m.visit[v[k]] : ~0ull;
@@ -3058,6 +3166,10 @@ __device__ __forceinline__ void ms_sssp_chunk(const MsArgs &m, const RegionArgs 
         o = (uint32_t)lo;
         ms_sssp_load_edge(a, (uint64_t)sm.start[o] + (e - sm.pref[o]), v, w);
         f = sm.f[o];
+        if (ASC_BAD(v >= m.V || (f >> 1 >> (R - 1)) != 0, 8, v)) {
+            v = 0;
+            f = 0;
+        }
     }
     const int nsrc = __popcll(f);
     const bool dense = nsrc > kMsQuadSources, mid = nsrc > kMsSparseSources && !dense;
@@ -3182,7 +3294,7 @@ __device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, u
     unsigned long long f = 0;
     bool seg = w < nseg;
     if (seg) {
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && !ASC_BAD((uint32_t)(a.seg_in[w] >> 32) >= m.V, 7, a.seg_in[w] >> 32)) {
             const uint64_t item = a.seg_in[w];
             const uint32_t k0 = (uint32_t)item;
             u = (uint32_t)(item >> 32);
@@ -3195,7 +3307,7 @@ __device__ void ms_sssp_item(const MsArgs &m, const RegionArgs &a, uint32_t w, u
         }
     } else {
         const uint32_t i = (w - nseg) * kBlock + threadIdx.x;
-        if (i < n_in) {
+        if (i < n_in && !ASC_BAD(a.q_in[i] >= m.V, 7, a.q_in[i])) {
             u = a.q_in[i];
             start = a.ptr[u];
             deg = a.ptr[u + 1] - start;
@@ -3295,7 +3407,8 @@ __global__ void ms_apply_kernel(MsArgs m, uint32_t **planes, const int32_t *lvl_
                 while (un) {
                     const int src = __ffsll((long long)un) - 1;
                     un &= un - 1;
-                    if ((nb >> src) & 1ull) planes[src][v] = (uint32_t)((int32_t)it + lvl_off[src]);
+                    if (((nb >> src) & 1ull) && !ASC_BAD(!planes[src], 12, src))
+                        planes[src][v] = (uint32_t)((int32_t)it + lvl_off[src]);
                 }
             }
             const unsigned nbits = __ballot_sync(kFull, nb != 0ull);
@@ -3361,7 +3474,7 @@ __global__ void cb_clear_kernel(unsigned long long *visit, uint32_t *dist, uint3
         while (t) {
             const int s = __ffsll((long long)t) - 1;
             t &= t - 1;
-            planes[s][v] = fill;
+            if (!ASC_BAD(!planes[s], 11, s)) planes[s][v] = fill;
         }
     }
 }
@@ -3385,6 +3498,7 @@ __global__ void cb_admit_kernel(Admit ad, MsArgs m, RegionArgs cur, uint32_t **p
     const uint32_t i = threadIdx.x;
     if (i >= ad.n) return;
     const uint32_t s = ad.slot[i], v = ad.src[i];
+    if (ASC_BAD(v >= m.V || s >= stride || (!sssp && !planes[s]), 9, v)) return;
     const unsigned long long bit = 1ull << s;
     if (sssp) m.dist[(uint64_t)v * stride + s] = 1;
     else {
@@ -3400,10 +3514,12 @@ __global__ void cb_admit_kernel(Admit ad, MsArgs m, RegionArgs cur, uint32_t **p
     if (deg > cur.huge) {
         const uint32_t nseg = (deg + cur.seg_len - 1) / cur.seg_len;
         const uint32_t sb = atomicAdd(&cur.cnt_out[2 + od], nseg);
+        if (ASC_BAD((uint64_t)sb + nseg > (od ? cur.segcap_ondemand : cur.segcap_static), 10, sb)) return;
         uint64_t *dst = cur.seg_out + (od ? cur.segcap_static : 0) + sb;
         for (uint32_t k = 0; k < nseg; k++) dst[k] = ((uint64_t)v << 32) | k;
     } else {
         const uint32_t pos = atomicAdd(&cur.cnt_out[od], 1u);
+        if (ASC_BAD((od ? cur.S : 0) + pos >= (od ? cur.V : cur.S), 10, pos)) return;
         cur.q_out[(od ? cur.S : 0) + pos] = v;
     }
 }
@@ -3424,15 +3540,45 @@ uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride) {
 
 uint64_t batch_plane_bytes(asc_graph *g) { return 4ull * g->V; }
 
-// Device bytes a graph's single-query state needs (estimate before the first
-// run; exact afterwards), with the PageRank buffers when asked for.
+// Self-checking build: the first index check that failed since the last call
+// (after the launching stream was synchronized), as an error.
+asc_status self_check_result() {
+#ifdef ASC_SELF_CHECK
+    unsigned long long v = 0;
+    ASC_CUDA(cudaMemcpyFromSymbol(&v, g_self_check, sizeof(v)));
+    if (v) {
+        const unsigned long long zero = 0;
+        ASC_CUDA(cudaMemcpyToSymbol(g_self_check, &zero, sizeof(zero)));
+        return fail(ASC_ERR_CUDA, "self-check failed at site %u, index %u", (unsigned)(v >> 32), (unsigned)v);
+    }
+#endif
+    return ASC_OK;
+}
+
+// Device bytes a graph's single-query state needs (an upper bound before the
+// first run; exact afterwards), with the PageRank buffers when asked for.
 uint64_t workspace_bytes(asc_graph *g, bool pagerank) {
-    const uint64_t V = g->V;
-    uint64_t b = g->ws ? g->ws->device_bytes : 4 * V + 4 * 4 * (V / 32 + 2) + 8 * V + 8 * (g->E / 256 + 1024) + 4096;
+    const uint64_t V = g->V, E = g->E;
+    const Tuning t = g->ws ? g->ws->tune : (g->has_tuning ? g->tuning : Tuning());
+    uint64_t b;
+    if (g->ws) {
+        b = g->ws->device_bytes;
+    } else {
+        // alloc_workspace: values, two queues, five bitmaps, control words, and
+        // two segment lists plus the list of long-list vertices (a list of d >
+        // huge_degree edges is ceil(d / segment_edges) <= d / segment_edges + 1
+        // segments, and there are at most E / (huge_degree + 1) such lists)
+        const uint64_t huge = E / ((uint64_t)t.huge_degree + 1) + 1;
+        const uint64_t segs = E / std::max<uint32_t>(1, t.segment_edges) + huge;
+        b = 12 * V + 20 * (V / 32 + 2) + 4 * CTL_WORDS + 16 * segs + 4 * huge + 8 * 16;
+    }
     if (pagerank && (!g->ws || !g->ws->pr_rank)) b += 4ull * 8 * V;
-    // in-edge offsets of bottom-up BFS steps, allocated on the first BFS
-    const uint32_t bu = g->ws ? g->ws->tune.bu_div : (g->has_tuning ? g->tuning.bu_div : Tuning().bu_div);
-    if (!g->is_csc && bu && (!g->ws || !g->ws->in_ptr)) b += 4 * (V + 1) + 4 * (V / 32 + 2);
+    // in-edge offsets of bottom-up BFS steps, allocated on the first BFS (with
+    // the in-edges themselves when every out-edge is resident)
+    if (!g->is_csc && t.bu_div && (!g->ws || !g->ws->in_ptr)) {
+        b += 4 * (V + 1) + 4 * (V / 32 + 2);
+        if (g->static_edges >= E) b += 4 * (g->in_ebits == 32 ? std::max<uint64_t>(1, E) : (E * g->in_ebits + 31) / 32 + 1);
+    }
     return b;
 }
 
@@ -3520,6 +3666,13 @@ asc_status batch_admit(BatchEngine *b, uint32_t slot, uint32_t source) {
 
 bool batch_busy(const BatchEngine *b) { return b->active != 0; }
 
+// Drops every source of a batch whose launch or collection failed: the batch
+// is idle afterwards (its state is undefined until new sources are admitted).
+void batch_abort(BatchEngine *b) {
+    b->active = 0;
+    b->pend_n = 0;
+}
+
 uint32_t batch_slots(const BatchEngine *b) { return b->sssp ? b->stride : 64u; }
 
 // Applies the queued admissions and launches one iteration on the batch's
@@ -3589,6 +3742,7 @@ asc_status batch_launch(BatchEngine *b) {
 // no frontier left (their values are final).
 asc_status batch_collect(BatchEngine *b, uint64_t *finished) {
     ASC_CUDA(cudaStreamSynchronize(b->stream));
+    ASC_TRY(self_check_result());
     unsigned long long al = 0;
     memcpy(&al, b->ws.h_ctl + CTL_ALIVE, 8);
     *finished = b->active & ~al;
@@ -3752,6 +3906,7 @@ __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t ti
                 const uint64_t idx = (uint64_t)sm.start[lo] + (e - sm.pref[lo]);
                 v[k] = WORDS == 2 ? __ldg(a.edges + 2 * idx) : edge_word(a.edges, idx, a.ebits) >> a.wbits;
                 ck[k] = sm.c[lo];
+                if (ASC_BAD(v[k] >= a.V, 18, v[k])) v[k] = 0xffffffffu;
             }
         }
 #pragma unroll
@@ -3769,6 +3924,7 @@ __device__ void push_tile(const PushArgs<T> &p, const RegionArgs &a, uint32_t ti
 template <typename T, int WORDS>
 __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t item) {
     const uint32_t u = (uint32_t)(item >> 32), k0 = (uint32_t)item;
+    if (ASC_BAD(u >= a.V, 19, u)) return;
     const uint64_t b = (uint64_t)a.ptr[u] + (uint64_t)k0 * a.seg_len;
     const uint64_t e = min((uint64_t)a.ptr[u + 1], b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
@@ -3780,6 +3936,7 @@ __device__ void push_segment(const PushArgs<T> &p, const RegionArgs &a, uint64_t
             const uint32_t j = base + k * kBlock + threadIdx.x;
             v[k] = j < n ? (WORDS == 2 ? __ldg(a.edges + 2 * (b + j)) : edge_word(a.edges, b + j, a.ebits) >> a.wbits)
                          : 0xffffffffu;
+            if (v[k] != 0xffffffffu && ASC_BAD(v[k] >= a.V, 18, v[k])) v[k] = 0xffffffffu;
         }
 #pragma unroll
         for (int k = 0; k < kUnroll; k++)

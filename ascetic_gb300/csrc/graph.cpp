@@ -491,6 +491,7 @@ static void destroy(asc_graph *g) {
     if (g->h_outdeg) cudaFreeHost(g->h_outdeg);
     if (g->h_in_edges) cudaFreeHost(g->h_in_edges);
     delete[] g->h_in_ptr;
+    delete[] g->h_in_none;
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }

@@ -22,6 +22,7 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -46,6 +47,8 @@ struct Query {
     uint32_t batch = 1;
     int32_t iterations = 0;
     bool cancel = false;
+    bool mem_wait = false;  // has waited for device memory (counted once)
+    std::string err;        // why the query failed (the worker's error message)
 };
 
 struct GraphSlot {
@@ -82,6 +85,7 @@ struct asc_server {
     std::thread batch_worker, single_worker;
     std::vector<double> lat_ms;
     uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, batches = 0, batch_sources = 0;
+    uint64_t engines_created = 0, engines_freed = 0, workspaces_freed = 0, memory_waits = 0;
     Clock::time_point first_submit, last_done;
     bool any_submit = false;
     asc_status fatal = ASC_OK;
@@ -131,6 +135,7 @@ void evict_idle_locked(asc_server *s) {
             asc::BatchEngine *b = gs.batch[k];
             if (!b || gs.in_use[k] || asc::batch_busy(b) || !gs.pend[k].empty()) continue;
             asc::batch_destroy(b);
+            s->engines_freed++;
             gs.batch[k] = nullptr;
             s->used_bytes -= gs.batch_bytes[k];
             gs.batch_bytes[k] = 0;
@@ -151,6 +156,7 @@ uint64_t reclaim_locked(asc_server *s, int keep) {
         GraphSlot &gs = s->graphs[gi];
         if ((int)gi == keep || (int)gi == s->single_graph || !gs.ws_bytes || !gs.g->ws) continue;
         asc::free_workspace(gs.g);
+        s->workspaces_freed++;
         s->used_bytes -= gs.ws_bytes;
         gs.ws_bytes = 0;
         gs.ws_pr = false;
@@ -196,6 +202,7 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
                     asc_status st = asc::batch_create(gs.g, sssp, stride, &b);
                     if (st == ASC_OK) {
                         gs.batch[k] = b;
+                        s->engines_created++;
                         gs.batch_bytes[k] = need;
                         s->used_bytes += need;
                     } else {
@@ -290,11 +297,19 @@ void batch_loop(asc_server *s) {
         }
         // finished sources: copy their values out
         std::vector<std::pair<Query *, asc_status>> done;
+        std::vector<std::string> why(work.size());
         for (size_t i = 0; i < work.size(); i++) {
             GraphSlot &gs = s->graphs[work[i].first];
             const int k = work[i].second;
             uint64_t f = fin[i];
             if (sts[i] != ASC_OK) {
+                // every source of the batch fails with the error; the engine is
+                // emptied so that it is freed below, not launched again
+                char msg[512];
+                asc_last_error(msg, sizeof(msg));
+                why[i] = std::string("graph ") + std::to_string(work[i].first) + (k ? " SSSP" : " BFS") +
+                         " batch: " + msg;
+                asc::batch_abort(gs.batch[k]);
                 for (uint32_t slot = 0; slot < 64; slot++)
                     if (gs.slot_q[k][slot]) f |= 1ull << slot;
             }
@@ -306,7 +321,16 @@ void batch_loop(asc_server *s) {
                 Query *q = gs.slot_q[k][slot];
                 if (!q) continue;
                 asc_status st = sts[i];
-                if (st == ASC_OK && q->out) st = asc::batch_fetch(gs.batch[k], slot, q->out, false);
+                if (st == ASC_OK && q->out) {
+                    st = asc::batch_fetch(gs.batch[k], slot, q->out, false);
+                    if (st != ASC_OK) {
+                        char msg[512];
+                        asc_last_error(msg, sizeof(msg));
+                        q->err = msg;
+                    }
+                } else if (st != ASC_OK) {
+                    q->err = why[i];
+                }
                 q->batch = width;
                 done.push_back({q, st});
                 gs.slot_q[k][slot] = nullptr;
@@ -314,6 +338,22 @@ void batch_loop(asc_server *s) {
         }
         lk.lock();
         for (const auto &w : work) s->graphs[w.first].in_use[w.second] = false;
+        // a batch whose launch failed is freed (its device state is undefined);
+        // its waiting queries get a new engine
+        for (size_t i = 0; i < work.size(); i++) {
+            GraphSlot &gs = s->graphs[work[i].first];
+            const int k = work[i].second;
+            if (sts[i] == ASC_OK || !gs.batch[k]) continue;
+            asc::batch_destroy(gs.batch[k]);
+            gs.batch[k] = nullptr;
+            s->used_bytes -= gs.batch_bytes[k];
+            gs.batch_bytes[k] = 0;
+            if (k == 0) {
+                s->used_bytes -= (uint64_t)gs.planes * 4ull * gs.g->V;
+                gs.planes = 0;
+            }
+            s->engines_freed++;
+        }
         for (auto &d : done) finish(s, d.first, d.second);
         s->batches += work.size();
         if (!done.empty()) s->cv_done.notify_all();
@@ -357,6 +397,8 @@ void single_loop(asc_server *s) {
                         continue;
                     }
                     // running batches still hold memory: retry when they drain
+                    if (!q->mem_wait) s->memory_waits++;
+                    q->mem_wait = true;
                     s->single.push_front(q);
                     s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
                     continue;
@@ -389,6 +431,12 @@ void single_loop(asc_server *s) {
         lk.unlock();
         asc_stats st;
         asc_status rc = asc_run(gs.g, q->algo, q->source, &q->params, q->out, &st);
+        std::string why;
+        if (rc != ASC_OK) {
+            char msg[512];
+            asc_last_error(msg, sizeof(msg));
+            why = std::string("graph ") + std::to_string(q->graph) + " whole run: " + msg;
+        }
         if (rc == ASC_OK && group.size() > 1) {
             size_t bytes = (size_t)gs.g->V *
                            (q->algo == ASC_PR ? ((q->params.pr_mode == ASC_PR_STD && q->params.precision == ASC_F32) ? 4 : 8)
@@ -398,10 +446,17 @@ void single_loop(asc_server *s) {
         }
         lk.lock();
         s->single_graph = -1;
+        // the run's state as allocated (an estimate is accounted before a
+        // graph's first run)
+        if (gs.g->ws && gs.g->ws->device_bytes != gs.ws_bytes) {
+            s->used_bytes = s->used_bytes - gs.ws_bytes + gs.g->ws->device_bytes;
+            gs.ws_bytes = gs.g->ws->device_bytes;
+        }
         s->cv_work.notify_all();
         for (Query *x : group) {
             x->iterations = st.iterations;
             x->batch = (uint32_t)group.size();
+            x->err = why;
             finish(s, x, rc);
         }
         s->cv_done.notify_all();
@@ -529,9 +584,11 @@ asc_status asc_server_wait(asc_server *s, uint64_t ticket, int64_t timeout_ms, a
         info->latency_ms = std::chrono::duration<double, std::milli>(q->t_end - q->t_submit).count();
     }
     asc_status st = q->status;
+    const std::string why = q->err;
     s->queries.erase(it);
     delete q;
-    if (st != ASC_OK && st != ASC_ERR_CANCELLED) return fail(st, "query %llu failed", (unsigned long long)ticket);
+    if (st != ASC_OK && st != ASC_ERR_CANCELLED)
+        return fail(st, "query %llu failed%s%s", (unsigned long long)ticket, why.empty() ? "" : ": ", why.c_str());
     return st;
 }
 
@@ -555,6 +612,10 @@ asc_status asc_server_stats_get(asc_server *s, asc_server_stats *out) {
     out->cancelled = s->cancelled;
     out->batch_iterations = s->batches;
     out->device_bytes = s->used_bytes;
+    out->engines_created = s->engines_created;
+    out->engines_freed = s->engines_freed;
+    out->workspaces_freed = s->workspaces_freed;
+    out->memory_waits = s->memory_waits;
     std::vector<double> l = s->lat_ms;
     if (!l.empty()) {
         std::sort(l.begin(), l.end());

@@ -222,6 +222,29 @@ def pr_study(args):
             g.run("pr", params=prm)
             r, st = g.run("pr", params=prm)
             res[name] = (r.astype(np.float64), st)
+        # host-link rate of the on-demand pull: 8 FP32 passes with the static and
+        # on-demand regions in separate launches timed apart; the on-demand
+        # launch reads the in-edges of the on-demand vertices whose lists are not
+        # cut into segments (longer lists go to the segmented kernel, untimed)
+        tun = g.get_tuning()
+        S = int(g.info.static_vertices)
+        deg = np.diff(cptr.astype(np.int64))
+        pull_edges = int(deg[S:][deg[S:] <= tun["huge_degree"]].sum())
+        del deg
+        prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32, max_iterations=8,
+                            flags=A.RUN_PHASE_TIMING | A.RUN_NO_OUTPUT)
+        _, st = g.run("pr", params=prm)
+        pull_bytes = pull_edges * g.info.edge_bits / 8.0 * st["iterations"]
+        gbs = pull_bytes / (st["ms_ondemand"] * 1e-3) / 1e9 if st["ms_ondemand"] else 0.0
+        peak = getattr(args, "link_gbs", 0.0) or 0.0
+        out["ondemand_pull_link"] = {
+            "kernel": "pr_pull_kernel<float> on-demand region (phase-timed passes)", "bound": "host-link",
+            "passes": st["iterations"], "bytes_per_pass": int(pull_bytes / max(1, st["iterations"])),
+            "ms_per_pass": round(st["ms_ondemand"] / max(1, st["iterations"]), 3),
+            "achieved": round(gbs, 1), "peak": round(peak, 1), "unit": "GB/s",
+            "frac": round(gbs / peak, 4) if peak else None,
+            "peak_source": "pinned H2D cudaMemcpyAsync measured in this run (asc_link_probe, 1 GiB, best of 3)",
+            "ms_static_per_pass": round(st["ms_static"] / max(1, st["iterations"]), 3)}
     t1 = time.perf_counter()
     exact, it, resid = oracle.pr_std_mt(cptr, ccol, od, oracle_threads())
     oracle_s = time.perf_counter() - t1
@@ -288,6 +311,29 @@ def pagerank_leg(args):
             g.run("pr", params=prm)
             r, st = g.run("pr", params=prm)
             res[name] = (r.astype(np.float64), st)
+        # host-link rate of the on-demand pull: 8 FP32 passes with the static and
+        # on-demand regions in separate launches timed apart; the on-demand
+        # launch reads the in-edges of the on-demand vertices whose lists are not
+        # cut into segments (longer lists go to the segmented kernel, untimed)
+        tun = g.get_tuning()
+        S = int(g.info.static_vertices)
+        deg = np.diff(cptr.astype(np.int64))
+        pull_edges = int(deg[S:][deg[S:] <= tun["huge_degree"]].sum())
+        del deg
+        prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32, max_iterations=8,
+                            flags=A.RUN_PHASE_TIMING | A.RUN_NO_OUTPUT)
+        _, st = g.run("pr", params=prm)
+        pull_bytes = pull_edges * g.info.edge_bits / 8.0 * st["iterations"]
+        gbs = pull_bytes / (st["ms_ondemand"] * 1e-3) / 1e9 if st["ms_ondemand"] else 0.0
+        peak = getattr(args, "link_gbs", 0.0) or 0.0
+        out["ondemand_pull_link"] = {
+            "kernel": "pr_pull_kernel<float> on-demand region (phase-timed passes)", "bound": "host-link",
+            "passes": st["iterations"], "bytes_per_pass": int(pull_bytes / max(1, st["iterations"])),
+            "ms_per_pass": round(st["ms_ondemand"] / max(1, st["iterations"]), 3),
+            "achieved": round(gbs, 1), "peak": round(peak, 1), "unit": "GB/s",
+            "frac": round(gbs / peak, 4) if peak else None,
+            "peak_source": "pinned H2D cudaMemcpyAsync measured in this run (asc_link_probe, 1 GiB, best of 3)",
+            "ms_static_per_pass": round(st["ms_static"] / max(1, st["iterations"]), 3)}
     stage = args.pr_stage_mib[-1] if args.pr_stage_mib else 128
     with A.Graph.from_csr(cptr, ccol, outdeg=od, budget=A.make_budget(frac=0.30, stage_bytes=stage << 20)) as g:
         prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32)
@@ -980,6 +1026,7 @@ def main():
     hbm_gbs = alg_s / (ms_s * 1e-3) / 1e9 if ms_s else 0.0
     link_bytes = eb * ed_o
     dma_gbs, smread_gbs = A.link_probe(1 << 30, 3)
+    args.link_gbs = dma_gbs
     link_gbs = link_bytes / (ms_o * 1e-3) / 1e9 if ms_o else 0.0
     # bottom-up: every unreached vertex reads its first in-edge from HBM
     # (bits(V - 1) per vertex) and probes the frontier bitmap (4 B); those whose

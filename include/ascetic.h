@@ -327,6 +327,10 @@ typedef struct asc_server_stats {
     double p50_ms, p99_ms, mean_ms, max_ms;  /* completed-query latency (the most recent 2^19..2^20) */
     double queries_per_s;   /* completed / (last completion - first submit) */
     double span_s;
+    uint64_t engines_created;   /* batch engines allocated */
+    uint64_t engines_freed;     /* batch engines freed (idle, or after a failed launch) */
+    uint64_t workspaces_freed;  /* single-query states of idle graphs freed for memory */
+    uint64_t memory_waits;      /* whole runs that waited for device memory held by batches */
 } asc_server_stats;
 
 void asc_server_config_default(asc_server_config *c);
