@@ -136,6 +136,10 @@ struct RegionArgs {
     uint32_t in_resident;         // in_edges is device memory (a graph without a cap), else pinned host
     const uint32_t *in_heads;     // first in-edge of every vertex in HBM (a bit stream of in_ebits), or null
     const uint32_t *in_none;      // one bit per vertex without in-edges (never reached but as a source)
+    // standard PageRank pull, on-demand region: tiles copy their in-edge range
+    // through shared memory (see pr_vertices); edge_words bounds those reads
+    uint32_t stage_edges;
+    uint64_t edge_words;
 };
 
 // True when this BFS iteration steps bottom-up: its input frontier (the
@@ -1072,9 +1076,15 @@ __device__ __forceinline__ void block_reduce2_atomic(double a, double b, double 
 #define ASC_PR_UNROLL 4
 #endif
 constexpr int kPrUnroll = ASC_PR_UNROLL;
+// Edge words a pull tile copies into shared memory per chunk (8 KB).
+#ifndef ASC_PR_STAGE_WORDS
+#define ASC_PR_STAGE_WORDS 2048
+#endif
+constexpr uint32_t kPrStageWords = ASC_PR_STAGE_WORDS;
 
 template <typename T>
 struct PrSmem {
+    alignas(16) uint32_t stage[kPrStageWords];
     uint32_t pref[kBlock + 1];
     uint32_t start[kBlock];
     uint32_t warp[kWarps + 1];
@@ -1082,6 +1092,95 @@ struct PrSmem {
     double red[2 * kWarps];
     uint32_t work;
 };
+
+// Sums the in-edge contributions of a standard-PageRank tile (consecutive
+// vertices, no long list, so their in-edges are one range [E0, E0 + total),
+// E0 = the first vertex's offset) with the range read through shared memory:
+// the CTA copies kPrStageWords edge words at a time with 16-byte loads, so
+// the host link serves runs of several KB per tile instead of one 128-byte
+// line per warp load, then every thread decodes its edges from shared memory
+// and gathers their contributions, kPrUnroll edges in flight. The summation
+// order is a fixed function of the range (same partials every pass).
+template <typename T>
+__device__ void pr_vertices_staged(const PrArgs<T> &p, uint32_t total, PrSmem<T> &sm) {
+    const RegionArgs &a = p.r;
+    const int lane = threadIdx.x & 31;
+    const uint32_t eb = a.ebits;
+    const uint64_t E0 = sm.start[0];
+    uint4 *st4 = reinterpret_cast<uint4 *>(sm.stage);
+    for (uint32_t c0 = 0; c0 < total;) {
+        // words [w_lo, w_end): edges [c0, c1) of the tile, w_lo 16-byte aligned
+        const uint64_t w_lo = (((E0 + c0) * eb) >> 5) & ~3ull;
+        const uint64_t cap_edges = (w_lo + kPrStageWords) * 32 / eb;  // edges ending in the chunk
+        const uint32_t c1 = (uint32_t)min((uint64_t)total, cap_edges - E0);
+        const uint64_t w_end = ((E0 + c1) * eb + 31) >> 5;
+        const uint32_t nq = (uint32_t)((w_end - w_lo + 3) >> 2);
+        for (uint32_t i = threadIdx.x; i < nq; i += kBlock) {
+            const uint64_t w = w_lo + 4ull * i;
+            uint4 q;
+            if (w + 4 <= a.edge_words) {
+                q = __ldg(reinterpret_cast<const uint4 *>(a.edges + w));
+            } else {  // the buffer's last words
+                q.x = w < a.edge_words ? __ldg(a.edges + w) : 0u;
+                q.y = w + 1 < a.edge_words ? __ldg(a.edges + w + 1) : 0u;
+                q.z = w + 2 < a.edge_words ? __ldg(a.edges + w + 2) : 0u;
+                q.w = 0u;
+            }
+            st4[i] = q;
+        }
+        __syncthreads();
+        const uint64_t bit0 = w_lo * 32;
+        for (uint32_t base = c0; base < c1; base += kPrUnroll * kBlock) {
+            T x[kPrUnroll];
+            int owner[kPrUnroll];
+            uint32_t srcv[kPrUnroll];
+#pragma unroll
+            for (int k = 0; k < kPrUnroll; k++) {
+                const uint32_t e = base + k * kBlock + threadIdx.x;
+                owner[k] = -1 - lane;  // distinct per invalid lane
+                srcv[k] = 0xffffffffu;
+                if (e < c1) {
+                    int lo = 0, hi = kBlock;
+                    while (hi - lo > 1) {
+                        int mid = (lo + hi) >> 1;
+                        if (sm.pref[mid] <= e) lo = mid;
+                        else hi = mid;
+                    }
+                    owner[k] = lo;
+                    const uint32_t bit = (uint32_t)((E0 + e) * eb - bit0);
+                    const uint32_t wi = bit >> 5, sh = bit & 31u;
+                    uint32_t v = sm.stage[wi] >> sh;
+                    if (eb < 32) {
+                        if (sh + eb > 32) v |= sm.stage[wi + 1] << (32 - sh);
+                        v &= (1u << eb) - 1u;
+                    }
+                    srcv[k] = v;
+                    if (ASC_BAD(srcv[k] >= a.V, 22, srcv[k])) {
+                        srcv[k] = 0xffffffffu;
+                        owner[k] = -1 - lane;
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kPrUnroll; k++) x[k] = srcv[k] != 0xffffffffu ? p.c_old[srcv[k]] : (T)0;
+#pragma unroll
+            for (int k = 0; k < kPrUnroll; k++) {
+                T xs = x[k];
+                const int ow = owner[k];
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    T y = __shfl_down_sync(kFull, xs, d);
+                    int oy = __shfl_down_sync(kFull, ow, d);
+                    if (lane + d < 32 && oy == ow) xs += y;
+                }
+                int oprev = __shfl_up_sync(kFull, ow, 1);
+                if (ow >= 0 && (lane == 0 || oprev != ow)) atomicAdd(&sm.sum[ow], PrAcc<T>::from(xs));
+            }
+        }
+        __syncthreads();  // the stage is rewritten by the next chunk
+        c0 = c1;
+    }
+}
 
 // Reference mode walks the active set like a traversal frontier (list, or
 // the bitmap in id order when dense) and a vertex that stays active sets its
@@ -1109,8 +1208,10 @@ __device__ void pr_vertices(const PrArgs<T> &p, bool valid, uint32_t u, PrSmem<T
     // kPrUnroll edges per thread per pass (edge k of a pass is edge
     // base + k * kBlock + thread): every source id is loaded, then every
     // contribution gathered, before any is summed, so a thread has kPrUnroll
-    // reads in flight over the host link (on-demand region) instead of one
-    for (uint32_t base = 0; base < total; base += kPrUnroll * kBlock) {
+    // reads in flight instead of one
+    const bool staged = !REF && a.stage_edges && !__syncthreads_or(valid && huge);
+    if (staged) pr_vertices_staged<T>(p, total, sm);
+    for (uint32_t base = 0; !staged && base < total; base += kPrUnroll * kBlock) {
         T x[kPrUnroll];
         int owner[kPrUnroll];
         uint32_t srcv[kPrUnroll];
@@ -1204,7 +1305,62 @@ __device__ void pr_segment(const PrArgs<T> &p, uint64_t item, PrSmem<T> &sm) {
     const uint64_t e = min((uint64_t)e0, b + a.seg_len);
     const uint32_t n = (uint32_t)(e - b);
     T x = (T)0;  // this thread's edges in order, then a fixed warp tree
-    for (uint32_t j0 = threadIdx.x; j0 < n; j0 += kPrUnroll * kBlock) {
+    if (a.stage_edges) {
+        // the segment's range through shared memory, as a staged tile: thread
+        // t still adds edges t, t + kBlock, ... in order
+        const uint32_t eb = a.ebits;
+        uint4 *st4 = reinterpret_cast<uint4 *>(sm.stage);
+        for (uint32_t c0 = 0; c0 < n;) {
+            const uint64_t w_lo = (((b + c0) * eb) >> 5) & ~3ull;
+            const uint64_t cap_edges = (w_lo + kPrStageWords) * 32 / eb;
+            const uint32_t c1 = (uint32_t)min((uint64_t)n, cap_edges - b);
+            const uint64_t w_end = ((b + c1) * eb + 31) >> 5;
+            const uint32_t nq = (uint32_t)((w_end - w_lo + 3) >> 2);
+            for (uint32_t i = threadIdx.x; i < nq; i += kBlock) {
+                const uint64_t w = w_lo + 4ull * i;
+                uint4 q;
+                if (w + 4 <= a.edge_words) {
+                    q = __ldg(reinterpret_cast<const uint4 *>(a.edges + w));
+                } else {
+                    q.x = w < a.edge_words ? __ldg(a.edges + w) : 0u;
+                    q.y = w + 1 < a.edge_words ? __ldg(a.edges + w + 1) : 0u;
+                    q.z = w + 2 < a.edge_words ? __ldg(a.edges + w + 2) : 0u;
+                    q.w = 0u;
+                }
+                st4[i] = q;
+            }
+            __syncthreads();
+            const uint64_t bit0 = w_lo * 32;
+            const uint32_t first = c0 + ((threadIdx.x + kBlock - c0 % kBlock) % kBlock);
+            for (uint32_t j0 = first; j0 < c1; j0 += kPrUnroll * kBlock) {
+                uint32_t sv[kPrUnroll];
+#pragma unroll
+                for (int k = 0; k < kPrUnroll; k++) {
+                    const uint32_t j = j0 + k * kBlock;
+                    sv[k] = 0xffffffffu;
+                    if (j < c1) {
+                        const uint32_t bit = (uint32_t)((b + j) * eb - bit0);
+                        const uint32_t wi = bit >> 5, sh = bit & 31u;
+                        uint32_t v = sm.stage[wi] >> sh;
+                        if (eb < 32) {
+                            if (sh + eb > 32) v |= sm.stage[wi + 1] << (32 - sh);
+                            v &= (1u << eb) - 1u;
+                        }
+                        sv[k] = ASC_BAD(v >= a.V, 23, v) ? 0xffffffffu : v;
+                    }
+                }
+                T c[kPrUnroll];
+#pragma unroll
+                for (int k = 0; k < kPrUnroll; k++) c[k] = sv[k] != 0xffffffffu ? p.c_old[sv[k]] : (T)0;
+#pragma unroll
+                for (int k = 0; k < kPrUnroll; k++)
+                    if (sv[k] != 0xffffffffu) x += c[k];
+            }
+            __syncthreads();
+            c0 = c1;
+        }
+    }
+    for (uint32_t j0 = threadIdx.x; !a.stage_edges && j0 < n; j0 += kPrUnroll * kBlock) {
         // kPrUnroll loads in flight, added in edge order
         uint32_t sv[kPrUnroll];
 #pragma unroll
@@ -1568,7 +1724,16 @@ RegionArgs region_args(asc_graph *g, Workspace *ws, int parity_in, int region, b
     }
     a.seg_in = ws->segs[parity_in] + (region == 0 ? 0 : ws->segcap_static);
     a.work = a.cnt_out + 4 + region;
+    a.edge_words = region == 0 ? edge_store_words(g, g->static_edges) : edge_store_words(g, g->E);
     return a;
+}
+
+// Standard PageRank pulls the on-demand region's tiles through shared memory
+// (pr_vertices_staged) on single-word edge layouts; ASC_PR_TILE_STAGE=0 reads
+// every edge word with its own load instead (for comparison).
+bool pr_tile_stage(const asc_graph *g) {
+    const char *env = getenv("ASC_PR_TILE_STAGE");
+    return g->edge_words == 1 && !(env && env[0] == '0');
 }
 
 RegionArgs region_args(asc_graph *g, int parity_in, int region, bool dense) {
@@ -2727,6 +2892,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
                 PrArgs<T> p0 = pa, p1 = pa;
                 p0.r = region_args(g, parity, 0, !REF);
                 p1.r = region_args(g, parity, 1, !REF);
+                p1.r.stage_edges = !REF && pr_tile_stage(g);
                 pr_pull_fused_kernel<T, REF>
                     <<<grid_for(ws, region_items[0] + region_items[1]), kBlock, 0, s>>>(p0, p1);
                 launches++;
@@ -2735,6 +2901,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
             for (int region = 0; region < 2; region++) {
                 if (!region_items[region]) continue;
                 pa.r = region_args(g, parity, region, !REF);
+                pa.r.stage_edges = region == 1 && !REF && pr_tile_stage(g);
                 ASC_TRY(pt.begin(region));
                 pt.record(s);
                 pr_pull_kernel<T, REF><<<grid_for(ws, region_items[region]), kBlock, 0, s>>>(pa);

@@ -398,7 +398,8 @@ static asc_status narrow_edges(asc_graph *g) {
     parallel_for(groups, host_threads(groups * 32), [&](unsigned, uint64_t b, uint64_t e) {
         for (uint64_t grp = b; grp < e; grp++) {
             uint32_t *out = packed + grp * bits;
-            for (uint32_t k = 0; k < bits; k++) out[k] = 0;
+            // a last, partial group ends inside the buffer's final words
+            for (uint32_t k = 0; k < bits && grp * bits + k < words; k++) out[k] = 0;
             const uint64_t i0 = grp * 32, n = std::min<uint64_t>(32, g->E - i0);
             for (uint32_t j = 0; j < n; j++) {
                 const uint32_t v = src[i0 + j], pos = j * bits, w = pos >> 5, sh = pos & 31;
@@ -433,7 +434,8 @@ static asc_status pack_stream(const uint32_t *src, uint64_t n, uint32_t bits, ui
     parallel_for(groups, host_threads(groups * 32), [&](unsigned, uint64_t b, uint64_t e) {
         for (uint64_t grp = b; grp < e; grp++) {
             uint32_t *o = packed + grp * bits;
-            for (uint32_t k = 0; k < bits; k++) o[k] = 0;
+            // a last, partial group ends inside the buffer's final words
+            for (uint32_t k = 0; k < bits && grp * bits + k < words; k++) o[k] = 0;
             const uint64_t i0 = grp * 32, m = std::min<uint64_t>(32, n - i0);
             for (uint32_t j = 0; j < m; j++) {
                 const uint32_t v = src[i0 + j], pos = j * bits, w = pos >> 5, sh = pos & 31;

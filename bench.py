@@ -224,17 +224,12 @@ def pr_study(args):
             res[name] = (r.astype(np.float64), st)
         # host-link rate of the on-demand pull: 8 FP32 passes with the static and
         # on-demand regions in separate launches timed apart; the on-demand
-        # launch reads the in-edges of the on-demand vertices whose lists are not
-        # cut into segments (longer lists go to the segmented kernel, untimed)
-        tun = g.get_tuning()
-        S = int(g.info.static_vertices)
-        deg = np.diff(cptr.astype(np.int64))
-        pull_edges = int(deg[S:][deg[S:] <= tun["huge_degree"]].sum())
-        del deg
+        # launch reads every in-edge of the on-demand vertices (tiles of short
+        # lists and the segments of long ones) over the host link
         prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32, max_iterations=8,
                             flags=A.RUN_PHASE_TIMING | A.RUN_NO_OUTPUT)
         _, st = g.run("pr", params=prm)
-        pull_bytes = pull_edges * g.info.edge_bits / 8.0 * st["iterations"]
+        pull_bytes = float(st["ondemand_bytes"])
         gbs = pull_bytes / (st["ms_ondemand"] * 1e-3) / 1e9 if st["ms_ondemand"] else 0.0
         peak = getattr(args, "link_gbs", 0.0) or 0.0
         out["ondemand_pull_link"] = {
@@ -313,17 +308,12 @@ def pagerank_leg(args):
             res[name] = (r.astype(np.float64), st)
         # host-link rate of the on-demand pull: 8 FP32 passes with the static and
         # on-demand regions in separate launches timed apart; the on-demand
-        # launch reads the in-edges of the on-demand vertices whose lists are not
-        # cut into segments (longer lists go to the segmented kernel, untimed)
-        tun = g.get_tuning()
-        S = int(g.info.static_vertices)
-        deg = np.diff(cptr.astype(np.int64))
-        pull_edges = int(deg[S:][deg[S:] <= tun["huge_degree"]].sum())
-        del deg
+        # launch reads every in-edge of the on-demand vertices (tiles of short
+        # lists and the segments of long ones) over the host link
         prm = A.make_params(pr_mode=A.PR_STD, precision=A.F32, max_iterations=8,
                             flags=A.RUN_PHASE_TIMING | A.RUN_NO_OUTPUT)
         _, st = g.run("pr", params=prm)
-        pull_bytes = pull_edges * g.info.edge_bits / 8.0 * st["iterations"]
+        pull_bytes = float(st["ondemand_bytes"])
         gbs = pull_bytes / (st["ms_ondemand"] * 1e-3) / 1e9 if st["ms_ondemand"] else 0.0
         peak = getattr(args, "link_gbs", 0.0) or 0.0
         out["ondemand_pull_link"] = {
