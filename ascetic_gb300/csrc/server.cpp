@@ -430,7 +430,12 @@ void single_loop(asc_server *s) {
         s->single_graph = (int)q->graph;
         lk.unlock();
         asc_stats st;
-        asc_status rc = asc_run(gs.g, q->algo, q->source, &q->params, q->out, &st);
+        // beside the batch worker, whole runs step their iterations from the
+        // host instead of a CUDA-graph loop: no graph is captured, launched or
+        // destroyed while the other worker allocates and frees device memory
+        asc_params prm = q->params;
+        if (s->cfg.mode == ASC_SERVE_BATCHED) prm.flags |= ASC_RUN_HOST_LOOP;
+        asc_status rc = asc_run(gs.g, q->algo, q->source, &prm, q->out, &st);
         std::string why;
         if (rc != ASC_OK) {
             char msg[512];
