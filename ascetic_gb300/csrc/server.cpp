@@ -8,7 +8,9 @@
 //    iterations (one edge read serves every source of the batch; batches of
 //    different graphs run on their own streams at the same time), and leave
 //    when their own frontier is empty. CC and PageRank queries run whole on a
-//    second worker; identical pending ones share one run.
+//    second worker; identical pending ones share one run. The two workers take
+//    turns on the device (one batch iteration, then one whole run, when both
+//    have work).
 //  - ASC_SERVE_FIFO: the plain engine, one query at a time in arrival order.
 // Admission accounts every device allocation against the budget: the graphs'
 // static regions and offsets, per-graph single-query state, batch state and
@@ -73,6 +75,16 @@ struct asc_server {
     asc_server_config cfg;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
+    // The two workers take turns on the device: one of them at a time has
+    // device work in flight or allocates and frees device memory (gpu_holder:
+    // 0 batch worker, 1 single worker, -1 neither); when both want it they
+    // alternate (gpu_last). Streams of the batch worker still overlap each
+    // other. The turn-taking went in after the GPU raised MMU faults (Xid 31)
+    // in a few sweeps of hundreds of queries with both workers' work in flight
+    // at once; one worker alone (the plain engine) never faulted.
+    std::condition_variable cv_gpu;
+    int gpu_holder = -1, gpu_last = -1;
+    bool gpu_want[2] = {false, false};
     std::vector<GraphSlot> graphs;
     std::map<uint64_t, Query *> queries;
     std::deque<Query *> single;     // CC / PR (batched mode) or everything (FIFO)
@@ -164,6 +176,21 @@ uint64_t reclaim_locked(asc_server *s, int keep) {
     return before - s->used_bytes;
 }
 
+// Waits for the device turn of worker `who` (lk holds s->mu).
+void gpu_acquire(asc_server *s, std::unique_lock<std::mutex> &lk, int who) {
+    s->gpu_want[who] = true;
+    s->cv_gpu.wait(lk, [&] { return s->gpu_holder < 0 && !(s->gpu_want[1 - who] && s->gpu_last == who); });
+    s->gpu_want[who] = false;
+    s->gpu_holder = who;
+}
+
+void gpu_release(asc_server *s, int who) {
+    if (s->gpu_holder != who) return;
+    s->gpu_holder = -1;
+    s->gpu_last = who;
+    s->cv_gpu.notify_all();
+}
+
 bool batchable(const asc_server *s, const Query *q) {
     return s->cfg.mode == ASC_SERVE_BATCHED && (q->algo == ASC_BFS || q->algo == ASC_SSSP);
 }
@@ -252,18 +279,26 @@ void batch_loop(asc_server *s) {
     if (s->device >= 0) cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
+        gpu_acquire(s, lk, 0);
         std::vector<std::pair<uint32_t, int>> work;
         admit_locked(s, work);
         if (work.empty()) {
-            if (s->stop) return;
+            if (s->stop) {
+                gpu_release(s, 0);
+                return;
+            }
             bool stalled = false;
             for (const auto &gs : s->graphs) stalled = stalled || !gs.pend[0].empty() || !gs.pend[1].empty();
             if (stalled) {
                 // queries wait for batch memory while no batch runs: free what
                 // is idle, else wait for the single worker's run, else run the
                 // waiting queries one at a time
-                if (reclaim_locked(s, -1) > 0) continue;
+                if (reclaim_locked(s, -1) > 0) {
+                    gpu_release(s, 0);
+                    continue;
+                }
                 if (s->single_graph >= 0) {
+                    gpu_release(s, 0);
                     s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
                     continue;
                 }
@@ -275,9 +310,11 @@ void batch_loop(asc_server *s) {
                         }
                 evict_idle_locked(s);
                 s->cv_work.notify_all();
+                gpu_release(s, 0);
                 continue;
             }
             s->cv_done.notify_all();
+            gpu_release(s, 0);
             s->cv_work.wait(lk);
             continue;
         }
@@ -357,6 +394,7 @@ void batch_loop(asc_server *s) {
         for (auto &d : done) finish(s, d.first, d.second);
         s->batches += work.size();
         if (!done.empty()) s->cv_done.notify_all();
+        gpu_release(s, 0);
     }
 }
 
@@ -370,9 +408,14 @@ void single_loop(asc_server *s) {
             s->cv_done.notify_all();
         }
         if (s->single.empty()) {
+            gpu_release(s, 1);
             if (s->stop) return;
             s->cv_work.wait(lk);
             continue;
+        }
+        if (s->gpu_holder != 1) {
+            gpu_acquire(s, lk, 1);
+            continue;  // the queue may have changed meanwhile
         }
         Query *q = s->single.front();
         s->single.pop_front();
@@ -386,6 +429,7 @@ void single_loop(asc_server *s) {
                 if (s->cfg.device_budget_bytes && need > s->cfg.device_budget_bytes) {
                     finish(s, q, ASC_ERR_BUDGET);
                     s->cv_done.notify_all();
+                    gpu_release(s, 1);
                     continue;
                 }
                 reclaim_locked(s, (int)q->graph);
@@ -394,12 +438,15 @@ void single_loop(asc_server *s) {
                     if (batch_held(s) == 0) {
                         finish(s, q, ASC_ERR_BUDGET);
                         s->cv_done.notify_all();
+                        gpu_release(s, 1);
                         continue;
                     }
                     // running batches still hold memory: retry when they drain
+                    // (the device turn goes to the batch worker meanwhile)
                     if (!q->mem_wait) s->memory_waits++;
                     q->mem_wait = true;
                     s->single.push_front(q);
+                    gpu_release(s, 1);
                     s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
                     continue;
                 }
@@ -430,12 +477,7 @@ void single_loop(asc_server *s) {
         s->single_graph = (int)q->graph;
         lk.unlock();
         asc_stats st;
-        // beside the batch worker, whole runs step their iterations from the
-        // host instead of a CUDA-graph loop: no graph is captured, launched or
-        // destroyed while the other worker allocates and frees device memory
-        asc_params prm = q->params;
-        if (s->cfg.mode == ASC_SERVE_BATCHED) prm.flags |= ASC_RUN_HOST_LOOP;
-        asc_status rc = asc_run(gs.g, q->algo, q->source, &prm, q->out, &st);
+        asc_status rc = asc_run(gs.g, q->algo, q->source, &q->params, q->out, &st);
         std::string why;
         if (rc != ASC_OK) {
             char msg[512];
@@ -465,6 +507,7 @@ void single_loop(asc_server *s) {
             finish(s, x, rc);
         }
         s->cv_done.notify_all();
+        gpu_release(s, 1);
     }
 }
 
