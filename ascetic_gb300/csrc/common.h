@@ -180,6 +180,17 @@ bool batch_busy(const BatchEngine *b);
 void batch_abort(BatchEngine *b);
 // Self-checking build (ASC_SELF_CHECK): the first failed device index check since the last call.
 asc_status self_check_result();
+// Called on the calling thread between the iterations of a host-stepped run
+// (and between PageRank passes), with none of the run's device work in flight:
+// the query server hands the device to its other worker there. Unset outside it.
+struct IterationHook {
+    void (*fn)(void *) = nullptr;
+    void *ctx = nullptr;
+};
+extern thread_local IterationHook t_iteration_hook;
+inline void iteration_boundary() {
+    if (t_iteration_hook.fn) t_iteration_hook.fn(t_iteration_hook.ctx);
+}
 // Source slots of a batch: 64, or the row width of a narrower SSSP batch.
 uint32_t batch_slots(const BatchEngine *b);
 asc_status batch_launch(BatchEngine *b);

@@ -2697,6 +2697,7 @@ asc_status run_traversal_impl(asc_graph *g, asc_algo algo, uint32_t source, cons
         memcpy(cnt, ws->h_ctl, sizeof(cnt));
         if (pt.on) ASC_TRY(pt.sum(phase_ms));
         parity = po;
+        iteration_boundary();
     }
     // a top-down BFS expands every reached vertex exactly once, so its
     // expansion counts already are the reached vertices and edges; SSSP
@@ -2928,6 +2929,7 @@ static asc_status pagerank_impl(asc_graph *g, const asc_params &p, void *out, as
         ASC_CUDA(cudaStreamSynchronize(s));
         if (pt.on) ASC_TRY(pt.sum(phase_ms));
         it++;
+        iteration_boundary();
         if (REF) {
             memcpy(cnt, ws->h_ctl, sizeof(cnt));
             parity = po;
@@ -3707,6 +3709,8 @@ uint64_t batch_state_bytes(asc_graph *g, bool sssp, uint32_t stride) {
 
 uint64_t batch_plane_bytes(asc_graph *g) { return 4ull * g->V; }
 
+thread_local IterationHook t_iteration_hook;
+
 // Self-checking build: the first index check that failed since the last call
 // (after the launching stream was synchronized), as an error.
 asc_status self_check_result() {
@@ -4282,6 +4286,7 @@ static asc_status pagerank_push_impl(asc_graph *g, const asc_params &p, void *ou
                                  cudaMemcpyDeviceToHost, s));
         ASC_CUDA(cudaStreamSynchronize(s));
         it++;
+        iteration_boundary();
         if (REF) {
             if (ws->h_ctl[0] == 0) break;
         } else {

@@ -191,6 +191,16 @@ void gpu_release(asc_server *s, int who) {
     s->cv_gpu.notify_all();
 }
 
+// Between two iterations of a whole run: the single worker hands the device to
+// the batch worker for one iteration when that one is waiting for it.
+void single_yield(void *ctx) {
+    asc_server *s = static_cast<asc_server *>(ctx);
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (!s->gpu_want[0]) return;
+    gpu_release(s, 1);
+    gpu_acquire(s, lk, 1);
+}
+
 bool batchable(const asc_server *s, const Query *q) {
     return s->cfg.mode == ASC_SERVE_BATCHED && (q->algo == ASC_BFS || q->algo == ASC_SSSP);
 }
@@ -477,7 +487,18 @@ void single_loop(asc_server *s) {
         s->single_graph = (int)q->graph;
         lk.unlock();
         asc_stats st;
-        asc_status rc = asc_run(gs.g, q->algo, q->source, &q->params, q->out, &st);
+        // beside the batch worker, a whole run steps its iterations from the
+        // host and gives the device turn to a waiting batch iteration between
+        // them, so a long run (PageRank on the largest graph: hundreds of ms)
+        // does not hold the batches up
+        asc_params prm = q->params;
+        if (s->cfg.mode == ASC_SERVE_BATCHED) {
+            prm.flags |= ASC_RUN_HOST_LOOP;
+            asc::t_iteration_hook.fn = single_yield;
+            asc::t_iteration_hook.ctx = s;
+        }
+        asc_status rc = asc_run(gs.g, q->algo, q->source, &prm, q->out, &st);
+        asc::t_iteration_hook = asc::IterationHook();
         std::string why;
         if (rc != ASC_OK) {
             char msg[512];
