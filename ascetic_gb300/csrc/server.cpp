@@ -140,6 +140,13 @@ uint64_t batch_held(const asc_server *s) {
     return b;
 }
 
+// Device bytes no reclaim frees: the graphs' static regions and offsets.
+uint64_t bases_total(const asc_server *s) {
+    uint64_t b = 0;
+    for (const auto &gs : s->graphs) b += gs.base_bytes;
+    return b;
+}
+
 // Frees the batch engines that have nothing running or waiting.
 void evict_idle_locked(asc_server *s) {
     for (auto &gs : s->graphs)
@@ -224,13 +231,13 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
                 // SSSP keeps a row of distances per vertex, one column per
                 // slot: rows of 64 sources, or of 32 or 16 where max_batch asks
                 // for no more or where 64 columns of this graph could never fit
-                // the budget
+                // the budget beside the graphs (idle batches and single-query
+                // state are freed for a waiting batch)
                 uint32_t stride = 64;
                 if (sssp) {
                     while (stride > 16 && stride / 2 >= max_batch) stride /= 2;
                     while (stride > 16 && s->cfg.device_budget_bytes &&
-                           asc::batch_state_bytes(gs.g, true, stride) + s->used_bytes - batch_held(s) >
-                               s->cfg.device_budget_bytes)
+                           asc::batch_state_bytes(gs.g, true, stride) + bases_total(s) > s->cfg.device_budget_bytes)
                         stride /= 2;
                 }
                 uint64_t need = asc::batch_state_bytes(gs.g, sssp, stride);
@@ -248,8 +255,7 @@ void admit_locked(asc_server *s, std::vector<std::pair<uint32_t, int>> &work) {
                             pend.pop_front();
                         }
                     }
-                } else if (s->cfg.device_budget_bytes && need + s->used_bytes - batch_held(s) >
-                                                            s->cfg.device_budget_bytes) {
+                } else if (s->cfg.device_budget_bytes && need + bases_total(s) > s->cfg.device_budget_bytes) {
                     // a batch of this graph can never fit: its queries run one at a time
                     while (!pend.empty()) {
                         s->single.push_back(pend.front());
