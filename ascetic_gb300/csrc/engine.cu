@@ -553,15 +553,26 @@ __global__ void __launch_bounds__(kBlock, ASC_EXPAND_MIN_BLOCKS) expand_fused_ke
 // One warp per 32-vertex bitmap word, lane = vertex: the warp writes the
 // word's reached and next-frontier bits whole. In-edges are read in place from
 // pinned host memory, kBuUnroll per lane before any frontier probe.
-constexpr int kBuUnroll = 4;
+#ifndef ASC_BU_UNROLL
+#define ASC_BU_UNROLL 4
+#endif
+constexpr int kBuUnroll = ASC_BU_UNROLL;
 
 // Words a warp takes per pass: all of their bitmap words, heads and frontier
 // probes are loaded before any is used, so a warp keeps that many independent
 // load chains in flight.
-constexpr int kBuWords = 4;
-// CTAs per SM the bottom-up kernel is compiled for (38 registers, no spill at
-// 4 words per pass); its grid is one wave of them.
-constexpr int kBuMinBlocks = 6;
+#ifndef ASC_BU_WORDS
+#define ASC_BU_WORDS 4
+#endif
+constexpr int kBuWords = ASC_BU_WORDS;
+// CTAs per SM the bottom-up kernel is compiled for; its grid is one wave of
+// them. RMAT scale 24, 25% budget: 352.4 GTEPS at 8 (32 registers), 336.4 at 6
+// (40), 303.8 at 4 (48); with 2 in-edges per scan step instead of 4, 351.0; with
+// 2 words per pass, 335.6 (all at 6 except the first).
+#ifndef ASC_BU_MIN_BLOCKS
+#define ASC_BU_MIN_BLOCKS 8
+#endif
+constexpr int kBuMinBlocks = ASC_BU_MIN_BLOCKS;
 
 __global__ void __launch_bounds__(kBlock, kBuMinBlocks) bottom_up_kernel(RegionArgs a, uint32_t nwords) {
     if (!bottom_up_step(a)) return;
