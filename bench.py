@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default thresholds instead of autotuning each graph before its timed runs")
+    ap.add_argument("--bfs-tuning", default="",
+                    help="huge_degree,segment_edges,dense_div,ctas_per_sm,bu_div: set the headline graph's BFS "
+                         "thresholds instead of autotuning them (so a profiler run uses the thresholds of a "
+                         "plain run; ncu distorts the autotuner's timings)")
     ap.add_argument("--split", action="store_true",
                     help="profiling aid: time the steps with one launch per region (phase timing)")
     ap.add_argument("--batch", type=int, default=64,
@@ -933,7 +937,12 @@ def main():
     # the autotuner picks the thresholds on sources other than the timed ones
     tune_srcs = pick_sources(ptr, 4, args.seed + 1000)
     t_tune = time.time()
-    tuning = None if args.no_tune else g.tune("bfs", tune_srcs, cache=False)
+    if args.bfs_tuning:
+        hd, sg, dd, cs, bu = (int(x) for x in args.bfs_tuning.split(","))
+        g.set_tuning(huge_degree=hd, segment_edges=sg, dense_div=dd, ctas_per_sm=cs, bu_div=bu)
+        tuning = g.get_tuning()
+    else:
+        tuning = None if args.no_tune else g.tune("bfs", tune_srcs, cache=False)
     t_tune = time.time() - t_tune
     nores = A.make_params(flags=A.RUN_NO_OUTPUT)
     for i in range(args.warmup):
