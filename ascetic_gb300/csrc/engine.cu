@@ -568,7 +568,8 @@ constexpr int kBuWords = ASC_BU_WORDS;
 // CTAs per SM the bottom-up kernel is compiled for; its grid is one wave of
 // them. RMAT scale 24, 25% budget: 352.4 GTEPS at 8 (32 registers), 336.4 at 6
 // (40), 303.8 at 4 (48); with 2 in-edges per scan step instead of 4, 351.0; with
-// 2 words per pass, 335.6 (all at 6 except the first).
+// 2 words per pass, 335.6 (all at 6 except the first). At 8, 2 in-edges per scan
+// step measured 330.6 against 343.5 for 4.
 #ifndef ASC_BU_MIN_BLOCKS
 #define ASC_BU_MIN_BLOCKS 8
 #endif
@@ -3023,7 +3024,6 @@ struct BatchEngine {
 
 namespace {
 
-constexpr int kMaxBatch = 64;
 enum { CTL_ALIVE = 34 };  // u64 (words 34-35): OR of the new frontier masks of an iteration
 
 struct MsArgs {
